@@ -1,0 +1,461 @@
+"""Benchmark: Born forward + RTM adjoint throughput on one GB300.
+
+One *step* is the hot path over one shot: the Born forward (rtmForward) plus
+the RTM adjoint (sourceProp + rtmAdjoint) of configuration c2 (256^3 model,
+368^3 compute grid, nt = 2000), i.e. 2 * N_interior * nt cell-updates.
+
+  value  device-timed Gcell-updates/s with every input resident in HBM
+  e2e    the same metric through the reference-facing C ABI
+         (gpu_funcs_3d.h names) with pinned host buffers, host<->device
+         copies inside the timed region, in the call order of
+         rtm_zero_op_3d.cc
+  roofline  achieved GB/s of the dominant kernel (the fused RTM adjoint
+         step) against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (C restatement of the reference cpuProp) on the
+         host cores, on a bounded sample of the same workload
+
+``--impl reference`` times the reference CPU implementation instead (the
+compiled reference where it exists on this machine, else the oracle port).
+Multi-GPU: shots are independent, so N ranks run N shots (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG_DIR = os.path.join(ROOT, "sc17-born_gb300")
+L2_BYTES = 129 * 2 ** 20
+FALLBACK_HBM_GBS = 6800.0
+# algorithmic bytes per interior cell-update (fp32, compulsory traffic)
+BYTES_PER_CELL = {"forward": 32, "source": 16, "adjoint": 40}
+
+
+def package():
+    if "born_gb300" in sys.modules:
+        return sys.modules["born_gb300"]
+    spec = importlib.util.spec_from_file_location(
+        "born_gb300", os.path.join(PKG_DIR, "__init__.py"),
+        submodule_search_locations=[PKG_DIR])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["born_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def workload_module():
+    spec = importlib.util.spec_from_file_location(
+        "born_gb300_workload", os.path.join(PKG_DIR, "workload.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        try:
+            d = json.load(open(path))
+            for k in ("hbm_gbs", "hbm_GBps", "hbm"):
+                if k in d:
+                    v = d[k]
+                    if isinstance(v, dict):
+                        v = v.get("burst", v.get("value"))
+                    return float(v), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_per_cell(kernel: str):
+    """DRAM bytes per interior cell-update of a kernel from the committed
+    ncu summary (profiles/<kernel>_dram.txt, line 'bytes_per_cell: X')."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_dram.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("bytes_per_cell:"):
+            return float(line.split(":")[1])
+    return None
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", "-i", str(self.index),
+                     f"--query-gpu={self.Q}", "--format=csv,noheader,nounits"],
+                    capture_output=True, text=True, timeout=5).stdout
+                self.rows.append([x.strip() for x in out.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for name, v in zip(names, r[4:8]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def barrier_max(value: float, world: int) -> float:
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.barrier()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(case, threads: int, kind: str, budget_s: float = 20.0):
+    """Gcell-updates/s of the CPU implementation on a truncated-nt sample of
+    the same grid: Born forward + source propagation + RTM adjoint."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    if kind == "reference" and po.ref_lib() is not None:
+        os.environ["ORACLE_REF_THREADS"] = str(threads)
+        mk = po.RefProp
+    else:
+        kind = "port"
+        po.set_threads(threads)
+        mk = po.PortProp
+    n_int = (case["shape"][0] - 8) * (case["shape"][1] - 8) * (case["shape"][2] - 8)
+
+    def run(nt):
+        c = dict(case)
+        c["nt"] = nt
+        t0 = time.perf_counter()
+        po.run_case(mk(), c, which="all")
+        return time.perf_counter() - t0
+
+    probe_nt = 2
+    t = run(probe_nt)
+    per_step = t / probe_nt
+    nt = int(max(2, min(200, budget_s / max(per_step, 1e-9))))
+    t = run(nt)
+    rate = 2.0 * n_int * nt / t / 1e9
+    return {"value": round(rate, 4), "unit": "Gcell-updates/s",
+            "cores": threads, "kind": "reference" if kind == "reference" else "port",
+            "sample": f"{case['name']} grid {case['shape'][2]}x{case['shape'][1]}x"
+                      f"{case['shape'][0]}, Born forward + source propagation + "
+                      f"RTM adjoint over nt={nt} of {case['nt']} steps "
+                      f"({t:.1f} s)"}
+
+
+def run_reference_arm(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    born = package()
+    born.build()
+    wl = workload_module()
+    case = wl.prepare_shot(born, args.config)
+    threads = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    kind = "reference" if po.ref_lib() is not None else "port"
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(case, threads, kind, budget_s=args.cpu_budget /
+                       max(1, args.steps))
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = statistics.median(vals)
+    n_int = wl.interior_cells(case["shape"])
+    line = {
+        "metric": "Gcell-updates/s Born fwd+adj", "value": v,
+        "unit": "Gcell-updates/s", "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 2.0 * n_int * case["nt"] / (v * 1e9) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded, shapes of the config)",
+        "config": {"workload": f"{args.config}: 3D Born forward + RTM adjoint, "
+                   f"compute grid {case['shape'][2]}^3, nt={case['nt']}",
+                   "grid": list(case["shape"]), "nt": case["nt"]},
+        "cpu_baseline": dict(r, value=v),
+        "e2e": {"value": v, "unit": "Gcell-updates/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def run_gpu_arm(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = local if world > 1 else 0
+    torch.cuda.set_device(dev)
+    born = package()
+    born.lib()
+    wl = workload_module()
+    case = wl.prepare_shot(born, args.config)
+    nz, ny, nx = case["shape"]
+    nt, jt = case["nt"], case["jts"]
+    n_int = wl.interior_cells(case["shape"])
+    cells_per_step = 2 * n_int * nt
+
+    prop = born.Gb300Prop(dev)
+    if args.tile >= 0 or args.zseg > 0:
+        prop.set_tiling(args.tile, args.zseg)
+    prop.createSpace(case["d"], case["d"], case["d"], 50.0, 0.0005, 0.0005,
+                     nx, ny, nz)
+    prop.transferSincTableS(8, jt, case["table_s"])
+    prop.transferSincTableD(8, jt, case["table_d"])
+    prop.transferSourceFunc(9, case["nt_big"], case["locs_s"], case["src"])
+    prop.transferVelFunc1(nx, ny, nz, case["vel1"])
+    prop.transferVelFunc2(nx, ny, nz, case["vel2"])
+    rec = np.ascontiguousarray(case["rec_in"])
+    prop.transferReceiverFunc(case["rec_nx"], case["rec_ny"], case["nt_big"],
+                              case["locs_r"], rec)
+    prop.check(prop.lib.born_set_reflectivity(prop.h, born.fptr(case["refl"])))
+    stream = torch.cuda.ExternalStream(prop.stream, device=dev)
+
+    def device_step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        prop.rtm_forward_device(jt, nt)
+        if ev:
+            ev[1].record(stream)
+        prop.source_prop_device(jt, nt)
+        if ev:
+            ev[2].record(stream)
+        prop.rtm_adjoint_device(jt, nt, swap=1)
+        if ev:
+            ev[3].record(stream)
+
+    for _ in range(args.warmup):
+        device_step()
+    prop.synchronize()
+    launches0 = prop.launches
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(4)]
+           for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for k in range(args.steps):
+            device_step(evs[k])
+        stop.record(stream)
+        prop.synchronize()
+        torch.cuda.synchronize()
+    launches = prop.launches - launches0
+    t_ms = start.elapsed_time(stop)
+    t_ms = barrier_max(t_ms, world)
+    fwd_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
+    src_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
+    adj_ms = sum(e[2].elapsed_time(e[3]) for e in evs) / args.steps
+    value = world * cells_per_step * args.steps / (t_ms / 1e3) / 1e9
+
+    # roofline of the dominant kernel: the fused RTM adjoint step
+    peak, peak_kind = measured_peak()
+    adj_launch_ms = adj_ms / nt
+    achieved = BYTES_PER_CELL["adjoint"] * n_int / (adj_launch_ms / 1e3) / 1e9
+    tpc = traffic_per_cell("adjoint_step")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": (round(tpc * n_int) if tpc else None),
+                "kernel": "step_kernel<adjoint> (fused r+s step, image)",
+                "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": BYTES_PER_CELL["adjoint"] * n_int,
+                "avg_launch_ms": round(adj_launch_ms, 4)}
+    phases = {"forward_ms": round(fwd_ms, 2), "source_ms": round(src_ms, 2),
+              "adjoint_ms": round(adj_ms, 2),
+              "forward_GBps": round(BYTES_PER_CELL["forward"] * n_int * nt /
+                                    (fwd_ms / 1e3) / 1e9, 1),
+              "source_GBps": round(BYTES_PER_CELL["source"] * n_int * (nt + 1) /
+                                   (src_ms / 1e3) / 1e9, 1)}
+
+    # e2e through the reference-facing C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_measure(born, case, args, dev, cells_per_step, world)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample(case, os.cpu_count() or 1, "port",
+                         budget_s=args.cpu_budget)
+
+    if rank == 0:
+        line = {
+            "metric": "Gcell-updates/s Born fwd+adj", "value": round(value, 3),
+            "unit": "Gcell-updates/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(t_ms / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded, shapes of the config)",
+            "config": {"workload": f"{args.config}: 3D Born forward + RTM "
+                       f"adjoint, compute grid {nx}x{ny}x{nz}, nt={nt}, "
+                       "random-boundary source reconstruction",
+                       "grid": [nz, ny, nx], "nt": nt, "jt": jt,
+                       "interior_cells": n_int,
+                       "l2": "inputs larger than L2 (7 x %.0f MB fields)" %
+                             (nx * ny * nz * 4 / 1e6),
+                       "parallelism": f"shots x{world} (one per GPU)"},
+            "roofline": roofline, "phases": phases,
+            "clocks": clk.summary(), "gpu_launches": launches,
+            "e2e": e2e, "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def e2e_measure(born, case, args, dev, cells_per_step, world):
+    """Steps through the gpu_funcs_3d.h entry points with pinned buffers."""
+    import torch
+    L = born.lib()
+    nz, ny, nx = case["shape"]
+    nt, jt = case["nt"], case["jts"]
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float32, pin_memory=True)
+        t.numpy()[...] = a
+        return t
+
+    vel1, vel2 = pinned(case["vel1"]), pinned(case["vel2"])
+    src = pinned(case["src"])
+    rec_in = pinned(case["rec_in"])
+    rec_out = pinned(np.zeros_like(case["rec_in"]))
+    refl = pinned(case["refl"])
+    p0 = pinned(np.zeros(case["shape"], np.float32))
+    p1 = pinned(np.zeros(case["shape"], np.float32))
+    img = pinned(np.zeros(case["shape"], np.float32))
+    zeros_rec = pinned(np.zeros_like(case["rec_in"]))
+    locs_s = np.ascontiguousarray(case["locs_s"], np.int32)
+    locs_r = np.ascontiguousarray(case["locs_r"], np.int32)
+    ts = np.ascontiguousarray(case["table_s"], np.float32)
+    fp = lambda t: C.cast(t.data_ptr(), born._fp)  # noqa: E731
+
+    L.setup_cuda(1)
+    L.create_gpu_space(case["d"], case["d"], case["d"], 50.0, .0005, .0005,
+                       nx, ny, nz)
+    L.transfer_sinc_table_s(8, jt, born.fptr(ts))
+    L.set_ntblock(50)
+    L.transfer_sinc_table_d(8, jt, born.fptr(ts))
+    h = L.born_default_handle()
+    if args.tile >= 0 or args.zseg > 0:
+        L.born_set_tiling(h, args.tile, args.zseg)
+    field = nx * ny * nz * 4
+
+    def step():
+        # rtm_zero_op::adjoint per shot (rtm_zero_op_3d.cc:249-282)
+        L.transfer_source_func(9, case["nt_big"], born.iptr(locs_s), fp(src))
+        L.transfer_vel_func1(nx, ny, nz, fp(vel1))
+        L.transfer_vel_func2(nx, ny, nz, fp(vel2))
+        L.transfer_receiver_func(case["rec_nx"], case["rec_ny"],
+                                 case["nt_big"], born.iptr(locs_r), fp(rec_in))
+        L.source_prop(nx, ny, nz, False, True, fp(p0), fp(p1), jt, 9, nt)
+        img.zero_()
+        L.rtm_adjoint(nx, ny, nz, jt, fp(p1), fp(p0), fp(img), 9, nt)
+        # rtm_zero_op::forward per shot (rtm_zero_op_3d.cc:147-185)
+        L.transfer_receiver_func(case["rec_nx"], case["rec_ny"],
+                                 case["nt_big"], born.iptr(locs_r),
+                                 fp(zeros_rec))
+        L.rtm_forward(nx, ny, nz, jt, fp(refl), fp(rec_out), 9, nt,
+                      case["nt_big"], case["rec_nx"], case["rec_ny"])
+        rc = L.born_default_status()
+        if rc != 0:
+            raise RuntimeError(L.born_default_error().decode())
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    steps = max(1, args.e2e_steps)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    t = time.perf_counter() - t0
+    t = barrier_max(t, world)
+    rec_bytes = case["rec_in"].size * 4
+    h2d = (2 * field + case["src"].size * 4 + 2 * rec_bytes + field + field)
+    d2h = 2 * field + field + rec_bytes
+    return {"value": round(world * cells_per_step * steps / t / 1e9, 3),
+            "unit": "Gcell-updates/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "steps": steps,
+            "api": "gpu_funcs_3d.h entry points, pinned host buffers"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--tile", type=int, default=-1)
+    ap.add_argument("--zseg", type=int, default=0)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        print("note: warm-up raised to the minimum of 3", file=sys.stderr)
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,169 @@
+/*
+ * born_gb300 — C ABI of the GB300 (sm_103a) Born-modelling / RTM propagator.
+ *
+ * Two layers, both plain C (host pointers, sizes, int status codes):
+ *
+ *  1. Drop-in entry points with the exact names and signatures of the
+ *     reference's GPU C ABI, base/gpu/gpu_funcs_3d.h:4-37, as bound by
+ *     base/gpu_prop.cc:6-70.  They drive one process-wide default handle on
+ *     the current device; like the reference they return void, but instead
+ *     of exit(-1) (base/gpu/gpu_funcs_3d.cu:58-70) they record an error that
+ *     born_default_status() / born_default_error() report.
+ *
+ *  2. A handle-based API (born_*) with per-handle device state and one CUDA
+ *     stream per handle; every call returns BORN_OK (0) or a negative
+ *     BORN_E* code and never exits.  Handles are thread-compatible: use one
+ *     handle per host thread.
+ *
+ * Grid: compute grid [n3][n2][n1] float, n1 fastest, n1 a multiple of 4 and
+ * every n >= 9; the reference sizes it to multiples of 16
+ * (base/source_func_3d.cc:21-34).  Interior cells [4, n-4) are updated;
+ * sources and receivers must lie in the interior; n1*n2*n3 < 2^31.
+ * Velocities are given as v^2 dt^2 (base/vel_fd_3d.cc:125).
+ */
+#ifndef BORN_GB300_H
+#define BORN_GB300_H
+
+#ifndef __cplusplus
+#include <stdbool.h>
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define BORN_OK 0
+#define BORN_EINVAL (-1)   /* bad argument or size */
+#define BORN_ECUDA (-2)    /* CUDA runtime / driver error */
+#define BORN_ENOMEM (-3)   /* device allocation failed */
+#define BORN_ESTATE (-4)   /* call sequence violated (e.g. no grid yet) */
+#define BORN_ETIMEOUT (-5) /* a device-side wait gave up (bounded spin) */
+#define BORN_ENODEV (-6)   /* no usable CUDA device */
+
+typedef struct born_handle born_handle;
+
+/* ======================================================================
+ * 1. Reference-compatible entry points (base/gpu/gpu_funcs_3d.h)
+ * ====================================================================== */
+
+/* gpu_funcs_3d.h:7 (setup_cuda, gpu_funcs_3d.cu:21-56).  Creates the default
+ * handle on the current device.  This build drives one GPU per process;
+ * ngpus > 1 is accepted and recorded, shots are spread by the caller. */
+void setup_cuda(int ngpus);
+
+/* gpu_funcs_3d.h:35-36 (create_gpu_space, gpu_funcs_3d.cu:1286-1317).
+ * Grid sizes, 8th-order coefficients from the spacings, taper table. */
+void create_gpu_space(float d1, float d2, float d3, float bc_a, float bc_b,
+                      float bc_b_y, int nx, int ny, int nz);
+
+/* gpu_funcs_3d.h:18-21: ns rows x nsinc taps, row-major (gpu_prop.cc:15-24) */
+void transfer_sinc_table_s(int nsinc, int ns, float *tables);
+void transfer_sinc_table_d(int nsinc, int ns, float *tabled);
+
+/* gpu_funcs_3d.h:23-24: npts source points, traces [npts][nt] */
+void transfer_source_func(int npts, int nt, int *locs, float *vals);
+
+/* gpu_funcs_3d.h:25 (load_source): kept for link compatibility; no-op. */
+void load_source(int it);
+
+/* gpu_funcs_3d.h:26-29: nx*ny receivers, traces [nx*ny][nt] */
+void transfer_receiver_func(int nx, int ny, int nt, int *locs, float *vals);
+
+/* gpu_funcs_3d.h:31-33: v^2 dt^2 of the random-boundary (1) and plain (2)
+ * velocity models */
+void transfer_vel_func1(int nx, int ny, int nz, float *vel);
+void transfer_vel_func2(int nx, int ny, int nz, float *vel);
+
+/* gpu_funcs_3d.h:10-11 (source_prop, gpu_funcs_3d.cu:199-446).  nt+1 steps
+ * of source propagation (cpu_prop.cc:106-129).  The two final levels stay on
+ * the device for rtm_adjoint; when get_last is true and p0/p1 are non-null
+ * they are also copied to the host arrays, as cpuProp does. */
+void source_prop(int n1, int n2, int n3, bool damp, bool get_last, float *p0,
+                 float *p1, int jt, int npts, int nt);
+
+/* gpu_funcs_3d.h:13-14 (rtm_adjoint, gpu_funcs_3d.cu:832-1154).  Reverse-time
+ * RTM adjoint (cpu_prop.cc:56-96).  p0_s_cpu/p1_s_cpu name the two source
+ * levels: when they are the host arrays last given to source_prop (in either
+ * order) the device-resident levels are used in that order; other non-null
+ * arrays are uploaded.  The full padded image is accumulated onto img (zero
+ * on entry at every reference call site, rtm_zero_op_3d.cc:259). */
+void rtm_adjoint(int n1, int n2, int n3, int j, float *p0_s_cpu,
+                 float *p1_s_cpu, float *img, int npts, int nt);
+
+/* gpu_funcs_3d.h:15 (set_ntblock): trace blocking is not needed (traces
+ * stay resident); recorded only. */
+void set_ntblock(int nt);
+
+/* gpu_funcs_3d.h:16-17 (rtm_forward; the reference GPU body is commented
+ * out, gpu_funcs_3d.cu:448-804, so this follows cpuProp::rtmForward,
+ * cpu_prop.cc:22-54).  Born forward of img into the receiver traces, which
+ * are accumulated onto the traces last transferred and written to dat. */
+void rtm_forward(int n1, int n2, int n3, int jt, float *img, float *dat,
+                 int npts_src, int nt, int nt_big, int nx, int ny);
+
+/* Status of the last default-handle call (0 or a BORN_E* code) and its
+ * message; these replace the reference's exit(-1). */
+int born_default_status(void);
+const char *born_default_error(void);
+born_handle *born_default_handle(void);
+
+/* ======================================================================
+ * 2. Handle-based API
+ * ====================================================================== */
+
+/* Creates a handle on CUDA device `device` (its own non-blocking stream). */
+int born_create(int device, born_handle **out);
+int born_destroy(born_handle *h);
+const char *born_error_string(const born_handle *h);
+
+/* cpuProp::createSpace / create_gpu_space */
+int born_create_space(born_handle *h, float d1, float d2, float d3, float bc_a,
+                      float bc_b, float bc_y, int nx, int ny, int nz);
+/* which = 0: source table (transferSincTableS), 1: data table (…D) */
+int born_set_sinc_table(born_handle *h, int which, int nsinc, int jt,
+                        const float *table);
+int born_set_source_func(born_handle *h, int npts, int nt_big, const int *locs,
+                         const float *vals);
+int born_set_receiver_func(born_handle *h, int rec_nx, int rec_ny, int nt_big,
+                           const int *locs, const float *traces);
+/* slot 1: random-boundary model (vel1), slot 2: plain model (vel2) */
+int born_set_velocity(born_handle *h, int slot, int nx, int ny, int nz,
+                      const float *v2dt2);
+/* Reflectivity for the Born forward (the image the forward reads). */
+int born_set_reflectivity(born_handle *h, const float *img);
+
+/* Time loops.  Null host pointers leave results on the device, which is how
+ * a caller chains calls without host round trips. */
+int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
+                     float *p1_out);
+/* swap = 0: the adjoint's (src_p0, src_p1) are source_prop's (p0, p1);
+ * swap = 1: they are (p1, p0), which is how rtm_zero_op_3d.cc:272-282
+ * calls it.  img (in/out, nullable): the image is accumulated onto its
+ * contents, as cpuProp does (cpu_prop.cc:101); null starts from zero and
+ * leaves the image on the device. */
+int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap, float *img);
+int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out);
+
+/* Device results and state transfers (host arrays of n1*n2*n3 floats, or
+ * npts*nt_big for traces) */
+int born_get_image(born_handle *h, float *img_out);
+int born_get_traces(born_handle *h, float *traces_out);
+int born_get_source_levels(born_handle *h, float *p0_out, float *p1_out);
+int born_set_source_levels(born_handle *h, const float *p0, const float *p1);
+int born_zero_traces(born_handle *h);
+int born_synchronize(born_handle *h);
+
+/* Tuning: tile configuration index (0..born_tile_config_count()-1, or -1 for
+ * the built-in choice) and z-segment depth (0 = automatic). */
+int born_tile_config_count(void);
+int born_set_tiling(born_handle *h, int tile_cfg, int zseg);
+/* Kernels launched on this handle since creation (for accounting). */
+long long born_kernel_launches(const born_handle *h);
+/* Raw CUDA stream of the handle (cudaStream_t), for event timing. */
+void *born_stream(born_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BORN_GB300_H */

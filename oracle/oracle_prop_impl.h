@@ -1,0 +1,230 @@
+/*
+ * Oracle (test infrastructure only): the propagator time loops of the
+ * reference CPU path, restated in C.  Included twice by born_oracle.c: once
+ * with REAL=float (the parity oracle, same operation order as the reference)
+ * and once with REAL=double (the FP64 accuracy oracle).  Only the tests, the
+ * smoke check and the CPU-baseline leg of bench.py load this code.
+ *
+ * Reference: base/cpu_prop.cc (ntuhpc/sc17-born).  Every function cites the
+ * lines it follows.  Operation order is kept exactly (left-to-right sums, no
+ * fused multiply-add: compile with -ffp-contract=off) so that the float
+ * instance reproduces the compiled reference bit for bit.
+ */
+#ifndef REAL
+#error "define REAL and SFX before including oracle_prop_impl.h"
+#endif
+
+#define CAT_(a, b) a##b
+#define CAT(a, b) CAT_(a, b)
+#define FN(name) CAT(name, SFX)
+#define PROPT CAT(oracle_prop, SFX)
+
+/* Coefficient slots, base/cpu_prop.cc:6-18: slot 1/4/7/10 ("CZ") is applied
+ * to the +-n12 neighbours, 2/5/8/11 ("CX") to +-1, 3/6/9/12 ("CY") to +-nx. */
+#ifndef ORACLE_K_SLOTS
+#define ORACLE_K_SLOTS
+enum { K_C0 = 0, K_CZ1 = 1, K_CX1 = 2, K_CY1 = 3, K_CZ2 = 4, K_CX2 = 5,
+       K_CY2 = 6, K_CZ3 = 7, K_CX3 = 8, K_CY3 = 9, K_CZ4 = 10, K_CX4 = 11,
+       K_CY4 = 12 };
+#endif
+
+/* cpuProp::prop, base/cpu_prop.cc:224-253.  p0 <- v*(L p1) + p1 + p1 - p0
+ * over the interior [4, n-4) of every axis, in place into p0. */
+void FN(oracle_prop_step)(const PROPT *s, REAL *p0, const REAL *p1,
+                          const REAL *vel) {
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  const long long n12 = (long long)nx * ny;
+  const REAL *c = s->coeffs;
+#pragma omp parallel for schedule(static)
+  for (int i3 = 4; i3 < nz - 4; i3++) {
+    for (int i2 = 4; i2 < ny - 4; i2++) {
+      long long ii = (long long)i2 * nx + 4 + n12 * i3;
+      for (int i1 = 4; i1 < nx - 4; i1++, ii++) {
+        p0[ii] = vel[ii] *
+                     (c[K_C0] * p1[ii] + c[K_CX1] * (p1[ii - 1] + p1[ii + 1]) +
+                      c[K_CX2] * (p1[ii - 2] + p1[ii + 2]) +
+                      c[K_CX3] * (p1[ii - 3] + p1[ii + 3]) +
+                      c[K_CX4] * (p1[ii - 4] + p1[ii + 4]) +
+                      c[K_CY1] * (p1[ii - nx] + p1[ii + nx]) +
+                      c[K_CY2] * (p1[ii - 2 * nx] + p1[ii + 2 * nx]) +
+                      c[K_CY3] * (p1[ii - 3 * nx] + p1[ii + 3 * nx]) +
+                      c[K_CY4] * (p1[ii - 4 * nx] + p1[ii + 4 * nx]) +
+                      c[K_CZ1] * (p1[ii - n12] + p1[ii + n12]) +
+                      c[K_CZ2] * (p1[ii - 2 * n12] + p1[ii + 2 * n12]) +
+                      c[K_CZ3] * (p1[ii - 3 * n12] + p1[ii + 3 * n12]) +
+                      c[K_CZ4] * (p1[ii - 4 * n12] + p1[ii + 4 * n12])) +
+                 p1[ii] + p1[ii] - p0[ii];
+      }
+    }
+  }
+}
+
+/* cpuProp::damp, base/cpu_prop.cc:141-165.  edge = distance to the interior
+ * face, min over the three axes; cells with 0 <= edge < 40 are scaled. */
+void FN(oracle_damp)(const PROPT *s, REAL *p0, REAL *p1) {
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  const long long n12 = (long long)nx * ny;
+#pragma omp parallel for schedule(static)
+  for (int i3 = 4; i3 < nz - 4; i3++) {
+    int e3 = i3 - 4 < nz - 4 - i3 ? i3 - 4 : nz - 4 - i3;
+    for (int i2 = 4; i2 < ny - 4; i2++) {
+      int e2 = i2 - 4 < ny - 4 - i2 ? i2 - 4 : ny - 4 - i2;
+      if (e3 < e2) e2 = e3;
+      long long ii = (long long)i2 * nx + 4 + n12 * i3;
+      for (int i1 = 4; i1 < nx - 4; i1++, ii++) {
+        int e1 = i1 - 4 < nx - 4 - i1 ? i1 - 4 : nx - 4 - i1;
+        int edge = e2 < e1 ? e2 : e1;
+        if (edge >= 0 && edge < ORACLE_NBOUND) {
+          p0[ii] *= s->bound[edge];
+          p1[ii] *= s->bound[edge];
+        }
+      }
+    }
+  }
+}
+
+/* cpuProp::injectSource, base/cpu_prop.cc:166-179. */
+void FN(oracle_inject_source)(const PROPT *s, int id, int ii, REAL *p) {
+  if (id + 7 >= s->nt_src) return;
+  const REAL *t = s->table_s + (long long)ii * s->nsinc_s;
+  for (int i = 0; i < s->npts_s; i++) {
+    const REAL *v = s->source + (long long)s->nt_src * i + id;
+    p[s->locs_s[i]] += (REAL)s->dir / (REAL)s->jt *
+                       (t[0] * v[0] + t[1] * v[1] + t[2] * v[2] + t[3] * v[3] +
+                        t[4] * v[4] + t[5] * v[5] + t[6] * v[6] + t[7] * v[7]);
+  }
+}
+
+/* cpuProp::injectReceivers, base/cpu_prop.cc:180-197. */
+void FN(oracle_inject_receivers)(const PROPT *s, int id, int ii, REAL *p) {
+  if (id + 7 >= s->nt_rec) return;
+  const REAL sc = (REAL)s->dir / (REAL)s->jt;
+  const REAL *t = s->table_d + (long long)ii * s->nsinc_d;
+  for (int i = 0; i < s->nrec; i++) {
+    const REAL *v = s->rec + (long long)s->nt_rec * i + id;
+    p[s->locs_r[i]] +=
+        sc * (t[0] * v[0] + t[1] * v[1] + t[2] * v[2] + t[3] * v[3] +
+              t[4] * v[4] + t[5] * v[5] + t[6] * v[6] + t[7] * v[7]);
+  }
+}
+
+/* cpuProp::dataExtract, base/cpu_prop.cc:198-215. */
+void FN(oracle_data_extract)(const PROPT *s, int id, int ii, const REAL *p) {
+  if (id + 7 >= s->nt_rec) return;
+  const REAL *t = s->table_d + (long long)ii * s->nsinc_d;
+  for (int i = 0; i < s->nrec; i++) {
+    REAL *r = s->rec + (long long)s->nt_rec * i + id;
+    const REAL v = p[s->locs_r[i]];
+    for (int k = 0; k < 8; k++) r[k] += v * t[k];
+  }
+}
+
+/* cpuProp::imageAdd, base/cpu_prop.cc:216-223: the Born coupling.  The
+ * constant is a double literal in the reference, so the product and the sum
+ * are formed in double and rounded once on the store. */
+void FN(oracle_image_add)(const PROPT *s, const REAL *img, REAL *rec_field,
+                          const REAL *src_field) {
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < s->n123; i++)
+    rec_field[i] += .000001 * src_field[i] * img[i];
+}
+
+/* cpuProp::imageCondition, base/cpu_prop.cc:97-105. */
+void FN(oracle_image_condition)(const PROPT *s, const REAL *rec,
+                                const REAL *src, REAL *img) {
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < s->n123; i++) img[i] += src[i] * rec[i];
+}
+
+/* cpuProp::sourceProp, base/cpu_prop.cc:106-129.  nt+1 steps with vel1, no
+ * damping, injection at +1/jt into the new level.  For odd nt the reference
+ * copies p0 into p1 at the end (both then hold the same level). */
+void FN(oracle_source_prop)(PROPT *s, REAL *p0, REAL *p1, int jts, int nt) {
+  s->jt = jts;
+  s->dir = 1;
+  for (int it = 0; it <= nt; it++) {
+    int id = it / s->jt_s;
+    int ii = it - id * s->jt_s;
+    FN(oracle_prop_step)(s, p0, p1, s->vel1);
+    FN(oracle_inject_source)(s, id, ii, p0);
+    REAL *pt = p1;
+    p1 = p0;
+    p0 = pt;
+  }
+  if (nt % 2 == 1) memcpy(p1, p0, sizeof(REAL) * (size_t)s->n123);
+}
+
+/* cpuProp::rtmAdjoint, base/cpu_prop.cc:56-96.  Reverse time; the source
+ * field is rebuilt by back-propagation through vel1, the receiver field is
+ * propagated through vel2, damped and fed with the data at -1/jt. */
+void FN(oracle_rtm_adjoint)(PROPT *s, REAL *src_p0, REAL *src_p1, REAL *img,
+                            int jtd, int nt) {
+  (void)jtd; /* the reference uses the table's own jt (cpu_prop.cc:75) */
+  REAL *rec0 = (REAL *)calloc((size_t)s->n123, sizeof(REAL));
+  REAL *rec1 = (REAL *)calloc((size_t)s->n123, sizeof(REAL));
+  REAL *r_p0 = rec0, *r_p1 = rec1;
+  s->dir = -1;
+  for (int it = nt - 1; it >= 0; it--) {
+    int id_s = (it + 1) / s->jt_s;
+    int i_s = it + 1 - id_s * s->jt_s;
+    int id = it / s->jt_d;
+    int ii = it - id * s->jt_d;
+    if (it > 0) FN(oracle_prop_step)(s, r_p0, r_p1, s->vel2);
+    if (it < nt - 1) {
+      FN(oracle_prop_step)(s, src_p0, src_p1, s->vel1);
+      FN(oracle_inject_source)(s, id_s, i_s, src_p1);
+    }
+    FN(oracle_damp)(s, r_p0, r_p1);
+    FN(oracle_inject_receivers)(s, id, ii, r_p0);
+    FN(oracle_image_condition)(s, r_p0, src_p0, img);
+    REAL *pt = src_p0;
+    src_p0 = src_p1;
+    src_p1 = pt;
+    pt = r_p0;
+    r_p0 = r_p1;
+    r_p1 = pt;
+  }
+  free(rec0);
+  free(rec1);
+}
+
+/* cpuProp::rtmForward, base/cpu_prop.cc:22-54.  Born forward: background s
+ * and scattered r, both through vel2 and damped; source into s at +1/jt;
+ * r += 1e-6 s img; r sampled into the traces. */
+void FN(oracle_rtm_forward)(PROPT *s, int jt, const REAL *img, REAL *rec,
+                            int nt) {
+  s->jt = jt;
+  s->rec = rec;
+  REAL *b0 = (REAL *)calloc((size_t)s->n123, sizeof(REAL));
+  REAL *b1 = (REAL *)calloc((size_t)s->n123, sizeof(REAL));
+  REAL *b2 = (REAL *)calloc((size_t)s->n123, sizeof(REAL));
+  REAL *b3 = (REAL *)calloc((size_t)s->n123, sizeof(REAL));
+  REAL *r_p0 = b0, *r_p1 = b1, *s_p0 = b2, *s_p1 = b3;
+  s->dir = 1;
+  for (int it = 0; it < nt; it++) {
+    int id = it / jt;
+    int ii = it - id * jt;
+    FN(oracle_prop_step)(s, s_p0, s_p1, s->vel2);
+    FN(oracle_prop_step)(s, r_p0, r_p1, s->vel2);
+    FN(oracle_damp)(s, s_p0, s_p1);
+    FN(oracle_damp)(s, r_p0, r_p1);
+    FN(oracle_inject_source)(s, id, ii, s_p0);
+    FN(oracle_image_add)(s, img, r_p0, s_p0);
+    FN(oracle_data_extract)(s, id, ii, r_p0);
+    REAL *pt = s_p0;
+    s_p0 = s_p1;
+    s_p1 = pt;
+    pt = r_p0;
+    r_p0 = r_p1;
+    r_p1 = pt;
+  }
+  free(b0);
+  free(b1);
+  free(b2);
+  free(b3);
+}
+
+#undef FN
+#undef PROPT
+#undef CAT
+#undef CAT_

@@ -1,0 +1,375 @@
+"""born_gb300 — GB300-native Born modelling / RTM propagator (host side).
+
+The compute path is ``_build/libborn_gb300.so`` (hand-written sm_103a CUDA
+kernels behind the C ABI declared in ``include/born_gb300.h``).  This module
+binds that ABI with ctypes and mirrors the reference's propagator interface
+``baseProp`` (``base/base_prop.h:4-72``) as :class:`Gb300Prop`, with the same
+method names, argument meaning and call order as ``cpuProp`` / ``gpuProp``, so
+code written against the reference drives the GPU unchanged.  There is no CPU
+fallback: if the library cannot be loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libborn_gb300.so")
+
+BORN_OK = 0
+ERRORS = {-1: "EINVAL", -2: "ECUDA", -3: "ENOMEM", -4: "ESTATE",
+          -5: "ETIMEOUT", -6: "ENODEV"}
+
+
+class BornError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"born_gb300 {ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_fp = C.POINTER(C.c_float)
+_ip = C.POINTER(C.c_int)
+_vp = C.c_void_p
+
+# name -> (restype, argtypes); mirrors include/born_gb300.h
+_SIGS = {
+    # reference-compatible names (base/gpu/gpu_funcs_3d.h)
+    "setup_cuda": (None, [C.c_int]),
+    "create_gpu_space": (None, [C.c_float] * 6 + [C.c_int] * 3),
+    "transfer_sinc_table_s": (None, [C.c_int, C.c_int, _fp]),
+    "transfer_sinc_table_d": (None, [C.c_int, C.c_int, _fp]),
+    "transfer_source_func": (None, [C.c_int, C.c_int, _ip, _fp]),
+    "load_source": (None, [C.c_int]),
+    "transfer_receiver_func": (None, [C.c_int, C.c_int, C.c_int, _ip, _fp]),
+    "transfer_vel_func1": (None, [C.c_int, C.c_int, C.c_int, _fp]),
+    "transfer_vel_func2": (None, [C.c_int, C.c_int, C.c_int, _fp]),
+    "source_prop": (None, [C.c_int, C.c_int, C.c_int, C.c_bool, C.c_bool,
+                           _fp, _fp, C.c_int, C.c_int, C.c_int]),
+    "rtm_adjoint": (None, [C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp, _fp,
+                           C.c_int, C.c_int]),
+    "set_ntblock": (None, [C.c_int]),
+    "rtm_forward": (None, [C.c_int, C.c_int, C.c_int, C.c_int, _fp, _fp,
+                           C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "born_default_status": (C.c_int, []),
+    "born_default_error": (C.c_char_p, []),
+    "born_default_handle": (_vp, []),
+    # handle API
+    "born_create": (C.c_int, [C.c_int, C.POINTER(_vp)]),
+    "born_destroy": (C.c_int, [_vp]),
+    "born_error_string": (C.c_char_p, [_vp]),
+    "born_create_space": (C.c_int, [_vp] + [C.c_float] * 6 + [C.c_int] * 3),
+    "born_set_sinc_table": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _fp]),
+    "born_set_source_func": (C.c_int, [_vp, C.c_int, C.c_int, _ip, _fp]),
+    "born_set_receiver_func": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _ip,
+                                         _fp]),
+    "born_set_velocity": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int,
+                                    _fp]),
+    "born_set_reflectivity": (C.c_int, [_vp, _fp]),
+    "born_source_prop": (C.c_int, [_vp, C.c_int, C.c_int, _fp, _fp]),
+    "born_rtm_adjoint": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _fp]),
+    "born_rtm_forward": (C.c_int, [_vp, C.c_int, C.c_int, _fp]),
+    "born_get_image": (C.c_int, [_vp, _fp]),
+    "born_get_traces": (C.c_int, [_vp, _fp]),
+    "born_get_source_levels": (C.c_int, [_vp, _fp, _fp]),
+    "born_set_source_levels": (C.c_int, [_vp, _fp, _fp]),
+    "born_zero_traces": (C.c_int, [_vp]),
+    "born_synchronize": (C.c_int, [_vp]),
+    "born_tile_config_count": (C.c_int, []),
+    "born_set_tiling": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "born_kernel_launches": (C.c_longlong, [_vp]),
+    "born_stream": (_vp, [_vp]),
+    # host geometry (csrc/born_host.h)
+    "born_sinc_table": (C.c_int, [C.c_int, C.c_int, _fp]),
+    "born_calc_stability": (C.c_float, [C.c_float, C.c_float, C.c_float,
+                                        C.c_int, _ip]),
+    "born_compute_size": (C.c_int, [C.c_int, C.c_int, C.c_int]),
+    "born_source_geometry": (C.c_int, [C.c_float] * 9 + [
+        C.c_int, C.c_int, _fp, C.c_int, C.c_int, _ip, _fp]),
+    "born_wavelet_deriv": (C.c_int, [_fp, C.c_int, C.c_float, _fp]),
+    "born_receiver_geometry": (C.c_int, [C.c_int, C.c_int] + [C.c_float] * 11
+                               + [C.c_int, C.c_int, _ip]),
+    "born_rand_subspace": (C.c_int, [_fp, C.c_int, C.c_int, C.c_int] +
+                           [C.c_float] * 7 + [C.c_int] * 4 + [C.c_float] +
+                           [C.c_int] * 3 + [C.c_float] * 6 + [_fp]),
+    "born_laplac_forward": (C.c_int, [C.c_int, _fp, _fp, C.c_int, C.c_int,
+                                      C.c_int]),
+    "born_laplac_adjoint": (C.c_int, [C.c_int, _fp, _fp, C.c_int, C.c_int,
+                                      C.c_int]),
+    "born_deriv_forward": (C.c_int, [C.c_int, _fp, _fp, C.c_int, C.c_int,
+                                     C.c_int, C.c_float]),
+    "born_deriv_adjoint": (C.c_int, [C.c_int, _fp, _fp, C.c_int, C.c_int,
+                                     C.c_int, C.c_float]),
+    "born_map_data_forward": (C.c_int, [C.c_int, _fp, _fp, C.c_int, C.c_int,
+                                        C.c_int, C.c_int]),
+    "born_map_data_adjoint": (C.c_int, [C.c_int, _fp, _fp, C.c_int, C.c_int,
+                                        C.c_int, C.c_int]),
+    "born_extract_sub": (C.c_int, [_fp, C.c_int, C.c_int, C.c_int, _fp,
+                                   C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                   C.c_int]),
+    "born_add_image": (C.c_int, [_fp, C.c_int, C.c_int, C.c_int, _fp, C.c_int,
+                                 C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+}
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the CUDA library in-tree (nvcc, sm_103a)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "born_gb300_build", os.path.join(HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def lib():
+    """The loaded CUDA library; raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with "
+                "`python sc17-born_gb300/build.py` (needs nvcc)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def fptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous, "need C float32"
+    return a.ctypes.data_as(_fp)
+
+
+def iptr(a):
+    assert a.dtype == np.int32 and a.flags.c_contiguous, "need C int32"
+    return a.ctypes.data_as(_ip)
+
+
+def f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Handle:
+    """Owns one ``born_handle`` (one device, one stream)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = lib()
+        h = _vp()
+        rc = self.lib.born_create(device, C.byref(h))
+        if rc != BORN_OK:
+            raise BornError(rc, f"born_create(device={device}) failed")
+        self.h = h
+
+    def check(self, rc: int) -> int:
+        if rc != BORN_OK:
+            msg = self.lib.born_error_string(self.h)
+            raise BornError(rc, msg.decode() if msg else "")
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.born_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.born_kernel_launches(self.h))
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.born_stream(self.h) or 0)
+
+    def set_tiling(self, cfg: int = -1, zseg: int = 0):
+        self.check(self.lib.born_set_tiling(self.h, cfg, zseg))
+
+    def synchronize(self):
+        self.check(self.lib.born_synchronize(self.h))
+
+
+class Gb300Prop(Handle):
+    """GPU propagator with the baseProp interface (base/base_prop.h:4-72).
+
+    Semantics follow the reference CPU propagator ``cpuProp``
+    (``base/cpu_prop.cc``): the receiver array given to
+    ``transferReceiverFunc`` is retained and ``rtmForward`` accumulates the
+    modelled traces into it; ``sourceProp`` leaves the final two levels in
+    ``p0``/``p1`` (and on the device); ``rtmAdjoint`` accumulates into
+    ``img``.  Device state persists between calls, as in ``gpuProp``.
+    """
+
+    def __init__(self, device: int = 0):
+        super().__init__(device)
+        self._rec = None
+        self._src_arrays = (None, None)
+        self.shape = None
+
+    def setNtblock(self, nb: int):  # base_prop.h:10-13
+        pass
+
+    def createSpace(self, d1, d2, d3, bc_a, bc_b, bc_y, nx, ny, nz):
+        self.check(self.lib.born_create_space(self.h, d1, d2, d3, bc_a, bc_b,
+                                              bc_y, nx, ny, nz))
+        self.shape = (nz, ny, nx)
+
+    def transferSincTableS(self, nsinc, jts, table):
+        t = f32(np.asarray(table).reshape(-1))
+        self.check(self.lib.born_set_sinc_table(self.h, 0, nsinc, jts,
+                                                fptr(t)))
+
+    def transferSincTableD(self, nsinc, jtd, table):
+        t = f32(np.asarray(table).reshape(-1))
+        self.check(self.lib.born_set_sinc_table(self.h, 1, nsinc, jtd,
+                                                fptr(t)))
+
+    def transferSourceFunc(self, npts, nt_big, locs, vals):
+        l = np.ascontiguousarray(locs, np.int32)
+        v = f32(vals)
+        self.check(self.lib.born_set_source_func(self.h, npts, nt_big, iptr(l),
+                                                 fptr(v)))
+
+    def transferVelFunc1(self, nx, ny, nz, vloc):
+        self.check(self.lib.born_set_velocity(self.h, 1, nx, ny, nz,
+                                              fptr(f32(vloc))))
+
+    def transferVelFunc2(self, nx, ny, nz, vloc):
+        self.check(self.lib.born_set_velocity(self.h, 2, nx, ny, nz,
+                                              fptr(f32(vloc))))
+
+    def transferReceiverFunc(self, nx, ny, nt, locs, rec):
+        l = np.ascontiguousarray(locs, np.int32)
+        assert rec.dtype == np.float32 and rec.flags.c_contiguous
+        self._rec = rec
+        self.check(self.lib.born_set_receiver_func(self.h, nx, ny, nt, iptr(l),
+                                                   fptr(rec)))
+
+    def sourceProp(self, nx, ny, nz, damp, getLast, p0, p1, jts, npts, nt):
+        out0 = fptr(p0) if getLast and p0 is not None else None
+        out1 = fptr(p1) if getLast and p1 is not None else None
+        self.check(self.lib.born_source_prop(self.h, jts, nt, out0, out1))
+        self._src_arrays = (p0, p1)
+
+    def rtmAdjoint(self, n1, n2, n3, jtd, p0, p1, img, npts_s, nt):
+        a0, a1 = self._src_arrays
+        if p0 is a1 and p1 is a0:
+            swap = 1
+        elif p0 is a0 and p1 is a1:
+            swap = 0
+        else:  # levels supplied by the caller
+            self.check(self.lib.born_set_source_levels(self.h, fptr(f32(p0)),
+                                                       fptr(f32(p1))))
+            self._src_arrays = (p0, p1)
+            swap = 0
+        self.check(self.lib.born_rtm_adjoint(self.h, jtd, nt, swap,
+                                             fptr(img)))
+
+    def rtmForward(self, n1, n2, n3, jt, img, rec, npts, nt, nt_big, rec_nx,
+                   rec_ny):
+        self.check(self.lib.born_set_reflectivity(self.h, fptr(f32(img))))
+        target = self._rec if self._rec is not None else rec
+        self.check(self.lib.born_rtm_forward(self.h, jt, nt, fptr(target)))
+        if rec is not None and target is not rec:
+            rec[...] = target
+
+    # ---- device-resident variants (no host round trips) ----
+    def source_prop_device(self, jts, nt):
+        self.check(self.lib.born_source_prop(self.h, jts, nt, None, None))
+
+    def rtm_adjoint_device(self, jtd, nt, swap=1):
+        self.check(self.lib.born_rtm_adjoint(self.h, jtd, nt, swap, None))
+
+    def rtm_forward_device(self, jt, nt):
+        self.check(self.lib.born_rtm_forward(self.h, jt, nt, None))
+
+    def get_image(self):
+        out = np.empty(self.shape, np.float32)
+        self.check(self.lib.born_get_image(self.h, fptr(out)))
+        return out
+
+    def get_traces(self, like):
+        out = np.empty_like(like, dtype=np.float32)
+        self.check(self.lib.born_get_traces(self.h, fptr(out)))
+        return out
+
+    def zero_traces(self):
+        self.check(self.lib.born_zero_traces(self.h))
+
+
+# ---------------------------------------------------------------------------
+# host geometry (csrc/born_host.h)
+
+def _ck(rc):
+    if rc != BORN_OK:
+        raise BornError(rc, "host geometry call failed")
+
+
+def sinc_table(ntab: int, nsinc: int = 8) -> np.ndarray:
+    out = np.zeros((ntab, nsinc), np.float32)
+    _ck(lib().born_sinc_table(ntab, nsinc, fptr(out)))
+    return out
+
+
+def calc_stability(vmax, dmin, dt_data, nt_data):
+    nt = C.c_int(0)
+    dt = lib().born_calc_stability(vmax, dmin, dt_data, nt_data, C.byref(nt))
+    return float(dt), int(nt.value)
+
+
+def compute_size(n_model, nbound, fat=4):
+    return int(lib().born_compute_size(n_model, nbound, fat))
+
+
+def source_geometry(sx, sy, sz, o, d, n1, n2, wavelet, nts):
+    locs = np.zeros(9, np.int32)
+    vals = np.zeros((9, nts), np.float32)
+    w = f32(wavelet)
+    _ck(lib().born_source_geometry(sx, sy, sz, o[0], o[1], o[2], d[0], d[1],
+                                   d[2], n1, n2, fptr(w), w.size, nts,
+                                   iptr(locs), fptr(vals)))
+    return locs, vals
+
+
+def wavelet_deriv(raw, dt):
+    raw = f32(raw)
+    out = np.zeros_like(raw)
+    _ck(lib().born_wavelet_deriv(fptr(raw), raw.size, dt, fptr(out)))
+    return out
+
+
+def receiver_geometry(rec_nx, rec_ny, rx0, rdx, ry0, rdy, rz, o, d, n1, n2):
+    locs = np.zeros(rec_nx * rec_ny, np.int32)
+    _ck(lib().born_receiver_geometry(rec_nx, rec_ny, rx0, rdx, ry0, rdy, rz,
+                                     o[0], o[1], o[2], d[0], d[1], d[2], n1,
+                                     n2, iptr(locs)))
+    return locs
+
+
+def rand_subspace(vel, vo, vd, vmax, irand, nrand, dt, shape, o, d):
+    """vel: model velocity [vn3][vn2][vn1]; shape (n3, n2, n1) compute grid."""
+    vel = f32(vel)
+    vn3, vn2, vn1 = vel.shape
+    n3, n2, n1 = shape
+    out = np.zeros(shape, np.float32)
+    _ck(lib().born_rand_subspace(fptr(vel), vn1, vn2, vn3, vo[0], vo[1], vo[2],
+                                 vd[0], vd[1], vd[2], vmax, irand, nrand[0],
+                                 nrand[1], nrand[2], dt, n1, n2, n3, o[0],
+                                 o[1], o[2], d[0], d[1], d[2], fptr(out)))
+    return out

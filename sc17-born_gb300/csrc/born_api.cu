@@ -1,0 +1,875 @@
+// C ABI of the Born / RTM propagator (include/born_gb300.h).
+//
+// Host side of the hot path: per-handle device state, host->device
+// transfers, point maps for injection/extraction, TMA descriptors and the
+// three time loops.  The loops mirror the reference CPU propagator's pointer
+// rotation step for step (base/cpu_prop.cc:22-129) so that every kernel sees
+// the same levels the reference would; the arithmetic itself is in
+// born_step.cu.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/born_gb300.h"
+#include "born_step.cuh"
+
+using born::kModeAdjoint;
+using born::kModeForward;
+using born::kModeSource;
+using born::PointSet;
+using born::StepParams;
+
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t,
+                                  void *, const cuuint64_t *, const cuuint64_t *,
+                                  const cuuint32_t *, const cuuint32_t *,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                         cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// Device copy of one point set (sources or receivers).
+struct DevPoints {
+  int npts = 0, nt = 0;
+  int *plane_off = nullptr, *cell_head = nullptr, *slot_cell = nullptr,
+      *slot_index = nullptr;
+  float *traces = nullptr;
+  size_t traces_cap = 0;
+  void release() {
+    cudaFree(plane_off);
+    cudaFree(cell_head);
+    cudaFree(slot_cell);
+    cudaFree(slot_index);
+    cudaFree(traces);
+    *this = DevPoints();
+  }
+};
+
+}  // namespace
+
+struct born_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // grid
+  bool have_space = false;
+  int n1 = 0, n2 = 0, n3 = 0;
+  long long n123 = 0;
+  float coeffs[13] = {};
+  float bound[born::kNBound] = {};
+  // sinc tables (rows x 8)
+  int jt_s = 0, jt_d = 0;
+  std::vector<float> tab_s, tab_d;
+  int jt = 1;  // the reference's _jt: last jt given to a time loop
+  // device fields
+  float *vel1 = nullptr, *vel2 = nullptr;
+  float *s0 = nullptr, *s1 = nullptr;  // source levels (p0, p1 of source_prop)
+  float *r0 = nullptr, *r1 = nullptr;  // receiver / scattered levels
+  float *f0 = nullptr, *f1 = nullptr;  // forward background levels
+  float *img = nullptr, *refl = nullptr;
+  unsigned int *err_dev = nullptr;
+  bool have_vel1 = false, have_vel2 = false, have_refl = false;
+  DevPoints src, rec;
+  bool src_levels_valid = false;
+  const float *host_p0 = nullptr, *host_p1 = nullptr;
+  int tile_cfg = -1, zseg = 0;
+  long long launches = 0;
+  int ntblock = 0;
+  std::map<std::pair<const void *, int>, CUtensorMap> maps;
+};
+
+namespace {
+
+int fail(born_handle *h, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  return code;
+}
+
+#define CK(h, call)                                                          \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      return fail(h, e_ == cudaErrorMemoryAllocation ? BORN_ENOMEM           \
+                                                     : BORN_ECUDA,           \
+                  "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                  __LINE__);                                                 \
+  } while (0)
+
+void free_fields(born_handle *h) {
+  float **bufs[] = {&h->vel1, &h->vel2, &h->s0, &h->s1, &h->r0,
+                    &h->r1,   &h->f0,   &h->f1, &h->img, &h->refl};
+  for (float **b : bufs) {
+    cudaFree(*b);
+    *b = nullptr;
+  }
+  h->maps.clear();
+  h->have_space = h->have_vel1 = h->have_vel2 = h->have_refl = false;
+  h->src_levels_valid = false;
+}
+
+int set_device(born_handle *h) {
+  CK(h, cudaSetDevice(h->device));
+  return BORN_OK;
+}
+
+// Coefficients of cpuProp::createSpace (cpu_prop.cc:314-326): formed in
+// double, stored as float.  Slot 1/4/7/10 use d1, 2/5/8/11 d2, 3/6/9/12 d3.
+void make_coeffs(float *c, float d1, float d2, float d3) {
+  auto c00 = [](float d) { return 8.0 / (5.0 * (double)d * (double)d); };
+  c[0] = (float)(-1025.0 / 576.0 * (c00(d1) + c00(d2) + c00(d3)));
+  const double div[4] = {1.0, -8.0, 63.0, -896.0};
+  const float ds[3] = {d1, d2, d3};
+  for (int o = 0; o < 4; ++o)
+    for (int a = 0; a < 3; ++a) c[1 + 3 * o + a] = (float)(c00(ds[a]) / div[o]);
+}
+
+// Taper of cpu_prop.cc:329-332: b[i] = expf(-0.0005f (40 - i)), fixed table.
+void make_bound(float *b) {
+  const float bcb = .0005f, bca = 40.f;
+  for (int i = 0; i < born::kNBound; ++i) b[i] = expf(-bcb * (bca - i));
+}
+
+bool interior(const born_handle *h, long long loc) {
+  if (loc < 0 || loc >= h->n123) return false;
+  const long long n12 = (long long)h->n1 * h->n2;
+  const int z = (int)(loc / n12), y = (int)((loc % n12) / h->n1),
+            x = (int)(loc % h->n1);
+  return x >= 4 && x < h->n1 - 4 && y >= 4 && y < h->n2 - 4 && z >= 4 &&
+         z < h->n3 - 4;
+}
+
+// Builds the sorted slot list and per-plane head maps of a point set.
+int upload_points(born_handle *h, DevPoints &dp, int npts, int nt,
+                  const int *locs, const float *traces) {
+  if (npts < 0 || nt < 0 || (npts > 0 && (!locs || !traces)))
+    return fail(h, BORN_EINVAL, "bad point set (npts=%d nt=%d)", npts, nt);
+  for (int i = 0; i < npts; ++i)
+    if (!interior(h, locs[i]))
+      return fail(h, BORN_EINVAL,
+                  "point %d at cell %d is outside the interior [4, n-4)", i,
+                  locs[i]);
+  std::vector<int> order(npts);
+  for (int i = 0; i < npts; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return locs[a] < locs[b]; });
+  const long long n12 = (long long)h->n1 * h->n2;
+  std::vector<int> plane_off(h->n3, -1), slot_cell(npts), slot_index(npts);
+  std::vector<int> planes;
+  for (int s = 0; s < npts; ++s) {
+    slot_cell[s] = locs[order[s]];
+    slot_index[s] = order[s];
+    const int z = (int)(slot_cell[s] / n12);
+    if (plane_off[z] < 0) {
+      plane_off[z] = (int)(planes.size() * n12);
+      planes.push_back(z);
+    }
+  }
+  if ((long long)planes.size() * n12 >= (1ll << 31))
+    return fail(h, BORN_EINVAL, "points span too many planes");
+  std::vector<int> head(std::max<size_t>(1, planes.size() * n12), -1);
+  for (int s = npts - 1; s >= 0; --s) {
+    const int z = (int)(slot_cell[s] / n12);
+    head[plane_off[z] + (slot_cell[s] % n12)] = s;
+  }
+  int rc = set_device(h);
+  if (rc) return rc;
+  cudaStreamSynchronize(h->stream);
+  const size_t tbytes = (size_t)npts * nt * sizeof(float);
+  DevPoints nd;
+  nd.npts = npts;
+  nd.nt = nt;
+  CK(h, cudaMalloc(&nd.plane_off, sizeof(int) * h->n3));
+  CK(h, cudaMalloc(&nd.cell_head, sizeof(int) * head.size()));
+  CK(h, cudaMalloc(&nd.slot_cell, sizeof(int) * std::max(1, npts)));
+  CK(h, cudaMalloc(&nd.slot_index, sizeof(int) * std::max(1, npts)));
+  CK(h, cudaMalloc(&nd.traces, std::max<size_t>(4, tbytes)));
+  nd.traces_cap = tbytes;
+  CK(h, cudaMemcpy(nd.plane_off, plane_off.data(), sizeof(int) * h->n3,
+                   cudaMemcpyHostToDevice));
+  CK(h, cudaMemcpy(nd.cell_head, head.data(), sizeof(int) * head.size(),
+                   cudaMemcpyHostToDevice));
+  if (npts) {
+    CK(h, cudaMemcpy(nd.slot_cell, slot_cell.data(), sizeof(int) * npts,
+                     cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(nd.slot_index, slot_index.data(), sizeof(int) * npts,
+                     cudaMemcpyHostToDevice));
+    CK(h, cudaMemcpy(nd.traces, traces, tbytes, cudaMemcpyHostToDevice));
+  }
+  dp.release();
+  dp = nd;
+  return BORN_OK;
+}
+
+int get_map(born_handle *h, const float *buf, int cfg, CUtensorMap *out) {
+  auto key = std::make_pair((const void *)buf, cfg);
+  auto it = h->maps.find(key);
+  if (it != h->maps.end()) {
+    *out = it->second;
+    return BORN_OK;
+  }
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return fail(h, BORN_ECUDA, "cuTensorMapEncodeTiled unavailable");
+  int tx, ty;
+  born::tile_cfg_dims(cfg, &tx, &ty);
+  CUtensorMap m;
+  const cuuint64_t dims[3] = {(cuuint64_t)h->n1, (cuuint64_t)h->n2,
+                              (cuuint64_t)h->n3};
+  const cuuint64_t strides[2] = {(cuuint64_t)h->n1 * 4,
+                                 (cuuint64_t)h->n1 * h->n2 * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)(tx + 8), (cuuint32_t)(ty + 8), 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)buf, dims,
+                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    return fail(h, BORN_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  h->maps[key] = m;
+  *out = m;
+  return BORN_OK;
+}
+
+// Tiling: the configured one, else 64x16 tiles; z segments sized so that
+// the grid covers every SM a few times.
+void pick_tiling(born_handle *h, int nfields, int *cfg, int *zseg, int *tiles_x,
+                 int *tiles_y) {
+  int c = h->tile_cfg >= 0 ? h->tile_cfg : 0;
+  int tx, ty;
+  born::tile_cfg_dims(c, &tx, &ty);
+  *cfg = c;
+  *tiles_x = (h->n1 - 8 + tx - 1) / tx;
+  *tiles_y = (h->n2 - 8 + ty - 1) / ty;
+  const int nzi = h->n3 - 8;
+  if (h->zseg > 0) {
+    *zseg = std::min(h->zseg, nzi);
+    return;
+  }
+  int sms = 148;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  const size_t smem = born::step_smem_bytes(c, std::max(1, nfields));
+  int per_sm = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
+  per_sm = std::min(per_sm, 2048 / ((tx / 4) * ty));
+  const long long target = 2ll * sms * per_sm;
+  const long long tiles = (long long)(*tiles_x) * (*tiles_y);
+  long long nseg = std::max<long long>(1, (target + tiles - 1) / tiles);
+  nseg = std::min<long long>(nseg, std::max(1, nzi / 16));
+  *zseg = (int)((nzi + nseg - 1) / nseg);
+}
+
+PointSet point_view(const DevPoints &dp, int id, int ii,
+                    const std::vector<float> &tab, float scale, bool use) {
+  PointSet ps;
+  memset(&ps, 0, sizeof(ps));
+  ps.plane_off = dp.plane_off;
+  ps.cell_head = dp.cell_head;
+  ps.slot_cell = dp.slot_cell;
+  ps.slot_index = dp.slot_index;
+  ps.traces = dp.traces;
+  ps.npts = dp.npts;
+  ps.nt_trace = dp.nt;
+  ps.id = id;
+  ps.scale = scale;
+  ps.active = use && dp.npts > 0 && (id + 7 < dp.nt) ? 1 : 0;
+  if (ps.active)
+    for (int k = 0; k < 8; ++k) ps.tab[k] = tab[(size_t)ii * 8 + k];
+  return ps;
+}
+
+void base_params(born_handle *h, StepParams &p) {
+  memset(&p, 0, sizeof(p));
+  p.n1 = h->n1;
+  p.n2 = h->n2;
+  p.n3 = h->n3;
+  memcpy(p.c, h->coeffs, sizeof(p.c));
+  memcpy(p.bound, h->bound, sizeof(p.bound));
+  p.err = h->err_dev;
+}
+
+int launch(born_handle *h, int mode, bool pa, bool pb, const float *a_cur,
+           const float *b_cur, StepParams &p) {
+  const int nf = (pa ? 1 : 0) + (pb ? 1 : 0);
+  int cfg, zseg, tx, ty;
+  pick_tiling(h, nf, &cfg, &zseg, &tx, &ty);
+  p.tiles_x = tx;
+  p.tiles_y = ty;
+  p.zseg = zseg;
+  CUtensorMap ma, mb;
+  int rc = get_map(h, pa ? a_cur : (b_cur ? b_cur : h->s0), cfg, &ma);
+  if (rc) return rc;
+  rc = get_map(h, pb ? b_cur : (a_cur ? a_cur : h->s0), cfg, &mb);
+  if (rc) return rc;
+  CK(h, born::launch_step(mode, pa, pb, cfg, ma, mb, p, h->stream));
+  h->launches++;
+  return BORN_OK;
+}
+
+// Every this many steps the loops look at the device error word, so that a
+// kernel whose bounded wait gave up stops the loop instead of being followed
+// by thousands of launches that would each exit early.
+constexpr int kErrPollSteps = 256;
+
+int poll_error(born_handle *h, int step) {
+  if (step % kErrPollSteps != kErrPollSteps - 1) return BORN_OK;
+  unsigned int e = 0;
+  CK(h, cudaMemcpyAsync(&e, h->err_dev, sizeof(e), cudaMemcpyDeviceToHost,
+                        h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  if (e)
+    return fail(h, BORN_ETIMEOUT,
+                "a device-side wait gave up (error word 0x%x)", e);
+  return BORN_OK;
+}
+
+int check_ready(born_handle *h) {
+  if (!h) return BORN_EINVAL;
+  if (!h->have_space)
+    return fail(h, BORN_ESTATE, "create_space has not been called");
+  return set_device(h);
+}
+
+int check_device_error(born_handle *h) {
+  unsigned int e = 0;
+  CK(h, cudaMemcpyAsync(&e, h->err_dev, sizeof(e), cudaMemcpyDeviceToHost,
+                        h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  if (e) {
+    cudaMemsetAsync(h->err_dev, 0, sizeof(unsigned int), h->stream);
+    return fail(h, BORN_ETIMEOUT,
+                "a device-side wait gave up (error word 0x%x)", e);
+  }
+  return BORN_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// Handle API
+extern "C" {
+
+int born_create(int device, born_handle **out) {
+  if (!out) return BORN_EINVAL;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return BORN_ENODEV;
+  if (device < 0 || device >= n) return BORN_EINVAL;
+  born_handle *h = new born_handle();
+  h->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) !=
+          cudaSuccess ||
+      cudaMalloc(&h->err_dev, sizeof(unsigned int)) != cudaSuccess ||
+      cudaMemset(h->err_dev, 0, sizeof(unsigned int)) != cudaSuccess) {
+    delete h;
+    return BORN_ECUDA;
+  }
+  *out = h;
+  return BORN_OK;
+}
+
+int born_destroy(born_handle *h) {
+  if (!h) return BORN_OK;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  free_fields(h);
+  h->src.release();
+  h->rec.release();
+  cudaFree(h->err_dev);
+  cudaStreamDestroy(h->stream);
+  delete h;
+  return BORN_OK;
+}
+
+const char *born_error_string(const born_handle *h) {
+  return h ? h->err.c_str() : "null handle";
+}
+
+int born_create_space(born_handle *h, float d1, float d2, float d3, float bc_a,
+                      float bc_b, float bc_y, int nx, int ny, int nz) {
+  (void)bc_a;
+  (void)bc_b;
+  (void)bc_y;  // the reference's taper ignores them (cpu_prop.cc:329-331)
+  if (!h) return BORN_EINVAL;
+  if (nx < 9 || ny < 9 || nz < 9 || nx % 4 != 0)
+    return fail(h, BORN_EINVAL,
+                "grid %d x %d x %d: need every n >= 9 and nx %% 4 == 0", nx,
+                ny, nz);
+  if ((long long)nx * ny * nz >= (1ll << 31))
+    return fail(h, BORN_EINVAL, "grid too large (n123 >= 2^31)");
+  if (!(d1 > 0 && d2 > 0 && d3 > 0))
+    return fail(h, BORN_EINVAL, "spacings must be positive");
+  int rc = set_device(h);
+  if (rc) return rc;
+  cudaStreamSynchronize(h->stream);
+  free_fields(h);
+  h->src.release();
+  h->rec.release();
+  h->n1 = nx;
+  h->n2 = ny;
+  h->n3 = nz;
+  h->n123 = (long long)nx * ny * nz;
+  make_coeffs(h->coeffs, d1, d2, d3);
+  make_bound(h->bound);
+  const size_t bytes = (size_t)h->n123 * sizeof(float);
+  float **bufs[] = {&h->vel1, &h->vel2, &h->s0, &h->s1, &h->r0,
+                    &h->r1,   &h->f0,   &h->f1, &h->img, &h->refl};
+  for (float **b : bufs) {
+    cudaError_t e = cudaMalloc(b, bytes);
+    if (e != cudaSuccess) {
+      free_fields(h);
+      return fail(h, BORN_ENOMEM, "cudaMalloc of %zu bytes failed: %s", bytes,
+                  cudaGetErrorString(e));
+    }
+    CK(h, cudaMemsetAsync(*b, 0, bytes, h->stream));
+  }
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->have_space = true;
+  return BORN_OK;
+}
+
+int born_set_sinc_table(born_handle *h, int which, int nsinc, int jt,
+                        const float *table) {
+  if (!h) return BORN_EINVAL;
+  if (nsinc != 8 || jt < 1 || !table || (which != 0 && which != 1))
+    return fail(h, BORN_EINVAL, "sinc table: need nsinc == 8, jt >= 1");
+  std::vector<float> t(table, table + (size_t)jt * 8);
+  if (which == 0) {
+    h->tab_s = t;
+    h->jt_s = jt;
+  } else {
+    h->tab_d = t;
+    h->jt_d = jt;
+  }
+  return BORN_OK;
+}
+
+int born_set_source_func(born_handle *h, int npts, int nt_big, const int *locs,
+                         const float *vals) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  h->src_levels_valid = false;
+  return upload_points(h, h->src, npts, nt_big, locs, vals);
+}
+
+int born_set_receiver_func(born_handle *h, int rec_nx, int rec_ny, int nt_big,
+                           const int *locs, const float *traces) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (rec_nx < 0 || rec_ny < 0)
+    return fail(h, BORN_EINVAL, "bad receiver grid");
+  return upload_points(h, h->rec, rec_nx * rec_ny, nt_big, locs, traces);
+}
+
+int born_set_velocity(born_handle *h, int slot, int nx, int ny, int nz,
+                      const float *v) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (nx != h->n1 || ny != h->n2 || nz != h->n3 || !v || (slot != 1 && slot != 2))
+    return fail(h, BORN_EINVAL, "velocity: grid mismatch or bad slot");
+  float *dst = slot == 1 ? h->vel1 : h->vel2;
+  CK(h, cudaMemcpyAsync(dst, v, (size_t)h->n123 * 4, cudaMemcpyHostToDevice,
+                        h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  (slot == 1 ? h->have_vel1 : h->have_vel2) = true;
+  return BORN_OK;
+}
+
+int born_set_reflectivity(born_handle *h, const float *img) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (!img) return fail(h, BORN_EINVAL, "null reflectivity");
+  CK(h, cudaMemcpyAsync(h->refl, img, (size_t)h->n123 * 4,
+                        cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->have_refl = true;
+  return BORN_OK;
+}
+
+// cpuProp::sourceProp, cpu_prop.cc:106-129
+int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
+                     float *p1_out) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (nt < 0 || jts < 1) return fail(h, BORN_EINVAL, "nt < 0 or jts < 1");
+  if (!h->have_vel1) return fail(h, BORN_ESTATE, "vel1 not transferred");
+  if (h->jt_s < 1) return fail(h, BORN_ESTATE, "source sinc table missing");
+  h->jt = jts;
+  const size_t bytes = (size_t)h->n123 * 4;
+  CK(h, cudaMemsetAsync(h->s0, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->s1, 0, bytes, h->stream));
+  float *p0 = h->s0, *p1 = h->s1;
+  const float scale = 1 / (float)jts;
+  for (int it = 0; it <= nt; ++it) {
+    const int id = it / h->jt_s, ii = it - id * h->jt_s;
+    StepParams p;
+    base_params(h, p);
+    p.a_cur = p1;
+    p.a_old = p0;
+    p.a_vel = h->vel1;
+    p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
+    p.pb = point_view(h->src, 0, 0, h->tab_s, 0.f, false);
+    rc = launch(h, kModeSource, true, false, p1, nullptr, p);
+    if (!rc) rc = poll_error(h, it);
+    if (rc) return rc;
+    std::swap(p0, p1);
+  }
+  if (nt % 2 == 1)
+    CK(h, cudaMemcpyAsync(p1, p0, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  h->src_levels_valid = true;
+  if (p0_out) CK(h, cudaMemcpyAsync(p0_out, h->s0, bytes, cudaMemcpyDeviceToHost, h->stream));
+  if (p1_out) CK(h, cudaMemcpyAsync(p1_out, h->s1, bytes, cudaMemcpyDeviceToHost, h->stream));
+  if (p0_out || p1_out) return check_device_error(h);
+  return BORN_OK;
+}
+
+// cpuProp::rtmAdjoint, cpu_prop.cc:56-96
+int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap,
+                     float *img_out) {
+  (void)jtd;  // the data table's own jt indexes the traces (cpu_prop.cc:75)
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (nt < 1) return fail(h, BORN_EINVAL, "nt < 1");
+  if (!h->have_vel1 || !h->have_vel2)
+    return fail(h, BORN_ESTATE, "velocities not transferred");
+  if (h->jt_s < 1 || h->jt_d < 1)
+    return fail(h, BORN_ESTATE, "sinc tables missing");
+  if (!h->src_levels_valid)
+    return fail(h, BORN_ESTATE, "no source levels (run source_prop first)");
+  const size_t bytes = (size_t)h->n123 * 4;
+  CK(h, cudaMemsetAsync(h->r0, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->r1, 0, bytes, h->stream));
+  // cpuProp accumulates into the caller's image (cpu_prop.cc:101)
+  if (img_out)
+    CK(h, cudaMemcpyAsync(h->img, img_out, bytes, cudaMemcpyHostToDevice,
+                          h->stream));
+  else
+    CK(h, cudaMemsetAsync(h->img, 0, bytes, h->stream));
+  float *sp0 = swap ? h->s1 : h->s0, *sp1 = swap ? h->s0 : h->s1;
+  float *rp0 = h->r0, *rp1 = h->r1;
+  const float scale = -1 / (float)h->jt;
+  PointSet pending = point_view(h->src, 0, 0, h->tab_s, 0.f, false);
+  for (int it = nt - 1; it >= 0; --it) {
+    const int id_s = (it + 1) / h->jt_s, i_s = it + 1 - id_s * h->jt_s;
+    const int id = it / h->jt_d, ii = it - id * h->jt_d;
+    const bool pa = it > 0, pb = it < nt - 1;
+    StepParams p;
+    base_params(h, p);
+    p.a_cur = rp1;
+    p.a_old = rp0;
+    p.a_vel = h->vel2;
+    p.b_cur = sp1;
+    p.b_old = sp0;
+    p.b_vel = h->vel1;
+    p.img = h->img;
+    p.pa = point_view(h->rec, id, ii, h->tab_d, scale, true);
+    p.pb = pending;
+    rc = launch(h, kModeAdjoint, pa, pb, rp1, sp1, p);
+    if (!rc) rc = poll_error(h, nt - 1 - it);
+    if (rc) return rc;
+    // the source injection of this step goes into the current level, which
+    // the next step reads as its previous level (cpu_prop.cc:79-82)
+    pending = point_view(h->src, id_s, i_s, h->tab_s, scale, pb);
+    std::swap(sp0, sp1);
+    std::swap(rp0, rp1);
+  }
+  if (pending.active) {
+    CK(h, born::launch_point_inject(pending, h->src.npts, sp0, h->stream));
+    h->launches++;
+  }
+  if (img_out) {
+    CK(h, cudaMemcpyAsync(img_out, h->img, bytes, cudaMemcpyDeviceToHost,
+                          h->stream));
+    return check_device_error(h);
+  }
+  return BORN_OK;
+}
+
+// cpuProp::rtmForward, cpu_prop.cc:22-54
+int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (nt < 0 || jt < 1) return fail(h, BORN_EINVAL, "nt < 0 or jt < 1");
+  if (!h->have_vel2 || !h->have_refl)
+    return fail(h, BORN_ESTATE, "vel2 or reflectivity not transferred");
+  if (jt > h->jt_s || jt > h->jt_d)
+    return fail(h, BORN_EINVAL, "jt %d exceeds the sinc tables' rows", jt);
+  h->jt = jt;
+  const size_t bytes = (size_t)h->n123 * 4;
+  CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->r0, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->r1, 0, bytes, h->stream));
+  float *sp0 = h->f0, *sp1 = h->f1, *rp0 = h->r0, *rp1 = h->r1;
+  const float scale = 1 / (float)jt;
+  for (int it = 0; it < nt; ++it) {
+    const int id = it / jt, ii = it - id * jt;
+    StepParams p;
+    base_params(h, p);
+    p.a_cur = sp1;
+    p.a_old = sp0;
+    p.a_vel = h->vel2;
+    p.b_cur = rp1;
+    p.b_old = rp0;
+    p.b_vel = h->vel2;
+    p.img = h->refl;
+    p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
+    p.pb = point_view(h->rec, id, ii, h->tab_d, 0.f, true);
+    rc = launch(h, kModeForward, true, true, sp1, rp1, p);
+    if (!rc) rc = poll_error(h, it);
+    if (rc) return rc;
+    std::swap(sp0, sp1);
+    std::swap(rp0, rp1);
+  }
+  if (traces_out) {
+    CK(h, cudaMemcpyAsync(traces_out, h->rec.traces,
+                          (size_t)h->rec.npts * h->rec.nt * 4,
+                          cudaMemcpyDeviceToHost, h->stream));
+    return check_device_error(h);
+  }
+  return BORN_OK;
+}
+
+int born_get_image(born_handle *h, float *img_out) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (!img_out) return fail(h, BORN_EINVAL, "null output");
+  CK(h, cudaMemcpyAsync(img_out, h->img, (size_t)h->n123 * 4,
+                        cudaMemcpyDeviceToHost, h->stream));
+  return check_device_error(h);
+}
+
+int born_get_traces(born_handle *h, float *out) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (!out) return fail(h, BORN_EINVAL, "null output");
+  if (h->rec.npts)
+    CK(h, cudaMemcpyAsync(out, h->rec.traces,
+                          (size_t)h->rec.npts * h->rec.nt * 4,
+                          cudaMemcpyDeviceToHost, h->stream));
+  return check_device_error(h);
+}
+
+int born_get_source_levels(born_handle *h, float *p0_out, float *p1_out) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  const size_t bytes = (size_t)h->n123 * 4;
+  if (p0_out) CK(h, cudaMemcpyAsync(p0_out, h->s0, bytes, cudaMemcpyDeviceToHost, h->stream));
+  if (p1_out) CK(h, cudaMemcpyAsync(p1_out, h->s1, bytes, cudaMemcpyDeviceToHost, h->stream));
+  return check_device_error(h);
+}
+
+int born_set_source_levels(born_handle *h, const float *p0, const float *p1) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (!p0 || !p1) return fail(h, BORN_EINVAL, "null source level");
+  const size_t bytes = (size_t)h->n123 * 4;
+  CK(h, cudaMemcpyAsync(h->s0, p0, bytes, cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(h->s1, p1, bytes, cudaMemcpyHostToDevice, h->stream));
+  CK(h, cudaStreamSynchronize(h->stream));
+  h->src_levels_valid = true;
+  return BORN_OK;
+}
+
+int born_zero_traces(born_handle *h) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (h->rec.npts)
+    CK(h, cudaMemsetAsync(h->rec.traces, 0, (size_t)h->rec.npts * h->rec.nt * 4,
+                          h->stream));
+  return BORN_OK;
+}
+
+int born_synchronize(born_handle *h) {
+  if (!h) return BORN_EINVAL;
+  int rc = set_device(h);
+  if (rc) return rc;
+  return check_device_error(h);
+}
+
+int born_tile_config_count(void) { return born::tile_cfg_count(); }
+
+int born_set_tiling(born_handle *h, int cfg, int zseg) {
+  if (!h) return BORN_EINVAL;
+  if (cfg < -1 || cfg >= born::tile_cfg_count() || zseg < 0)
+    return fail(h, BORN_EINVAL, "bad tiling (%d, %d)", cfg, zseg);
+  h->tile_cfg = cfg;
+  h->zseg = zseg;
+  return BORN_OK;
+}
+
+long long born_kernel_launches(const born_handle *h) {
+  return h ? h->launches : 0;
+}
+
+void *born_stream(born_handle *h) { return h ? (void *)h->stream : nullptr; }
+
+// ===========================================================================
+// Reference-compatible entry points over a default handle
+namespace {
+born_handle *g_default = nullptr;
+int g_status = BORN_OK;
+std::string g_error;
+int g_ngpus = 1;
+
+void record(int rc) {
+  g_status = rc;
+  if (rc == BORN_OK)
+    g_error.clear();
+  else
+    g_error = g_default ? g_default->err : std::string("no device handle");
+}
+
+born_handle *dflt() {
+  if (!g_default) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int rc = born_create(dev, &g_default);
+    if (rc) {
+      g_default = nullptr;
+      record(rc);
+    }
+  }
+  return g_default;
+}
+}  // namespace
+
+int born_default_status(void) { return g_status; }
+const char *born_default_error(void) { return g_error.c_str(); }
+born_handle *born_default_handle(void) { return dflt(); }
+
+void setup_cuda(int ngpus) {
+  g_ngpus = ngpus;
+  record(dflt() ? BORN_OK : BORN_ENODEV);
+}
+
+void create_gpu_space(float d1, float d2, float d3, float bc_a, float bc_b,
+                      float bc_b_y, int nx, int ny, int nz) {
+  born_handle *h = dflt();
+  record(h ? born_create_space(h, d1, d2, d3, bc_a, bc_b, bc_b_y, nx, ny, nz)
+           : BORN_ENODEV);
+}
+
+void transfer_sinc_table_s(int nsinc, int ns, float *tables) {
+  born_handle *h = dflt();
+  record(h ? born_set_sinc_table(h, 0, nsinc, ns, tables) : BORN_ENODEV);
+}
+
+void transfer_sinc_table_d(int nsinc, int ns, float *tabled) {
+  born_handle *h = dflt();
+  record(h ? born_set_sinc_table(h, 1, nsinc, ns, tabled) : BORN_ENODEV);
+}
+
+void transfer_source_func(int npts, int nt, int *locs, float *vals) {
+  born_handle *h = dflt();
+  record(h ? born_set_source_func(h, npts, nt, locs, vals) : BORN_ENODEV);
+}
+
+void load_source(int it) { (void)it; }
+
+void transfer_receiver_func(int nx, int ny, int nt, int *locs, float *vals) {
+  born_handle *h = dflt();
+  record(h ? born_set_receiver_func(h, nx, ny, nt, locs, vals) : BORN_ENODEV);
+}
+
+void transfer_vel_func1(int nx, int ny, int nz, float *vel) {
+  born_handle *h = dflt();
+  record(h ? born_set_velocity(h, 1, nx, ny, nz, vel) : BORN_ENODEV);
+}
+
+void transfer_vel_func2(int nx, int ny, int nz, float *vel) {
+  born_handle *h = dflt();
+  record(h ? born_set_velocity(h, 2, nx, ny, nz, vel) : BORN_ENODEV);
+}
+
+void source_prop(int n1, int n2, int n3, bool damp, bool get_last, float *p0,
+                 float *p1, int jt, int npts, int nt) {
+  (void)damp;
+  (void)npts;
+  born_handle *h = dflt();
+  if (!h) return record(BORN_ENODEV);
+  if (h->have_space && (n1 != h->n1 || n2 != h->n2 || n3 != h->n3))
+    return record(fail(h, BORN_EINVAL, "source_prop: grid mismatch"));
+  int rc = born_source_prop(h, jt, nt, get_last ? p0 : nullptr,
+                            get_last ? p1 : nullptr);
+  if (rc == BORN_OK) {
+    h->host_p0 = p0;
+    h->host_p1 = p1;
+  }
+  record(rc);
+}
+
+void rtm_adjoint(int n1, int n2, int n3, int j, float *p0_s_cpu,
+                 float *p1_s_cpu, float *img, int npts, int nt) {
+  (void)npts;
+  born_handle *h = dflt();
+  if (!h) return record(BORN_ENODEV);
+  if (h->have_space && (n1 != h->n1 || n2 != h->n2 || n3 != h->n3))
+    return record(fail(h, BORN_EINVAL, "rtm_adjoint: grid mismatch"));
+  int swap = 0;
+  const bool resident = h->src_levels_valid && p0_s_cpu && p1_s_cpu;
+  if (resident && p0_s_cpu == h->host_p1 && p1_s_cpu == h->host_p0) {
+    swap = 1;
+  } else if (resident && p0_s_cpu == h->host_p0 && p1_s_cpu == h->host_p1) {
+    swap = 0;
+  } else if (p0_s_cpu && p1_s_cpu) {
+    int rc = born_set_source_levels(h, p0_s_cpu, p1_s_cpu);
+    if (rc) return record(rc);
+    h->host_p0 = p0_s_cpu;
+    h->host_p1 = p1_s_cpu;
+  }
+  record(born_rtm_adjoint(h, j, nt, swap, img));
+}
+
+void set_ntblock(int nt) {
+  born_handle *h = dflt();
+  if (h) h->ntblock = nt;
+  record(h ? BORN_OK : BORN_ENODEV);
+}
+
+void rtm_forward(int n1, int n2, int n3, int jt, float *img, float *dat,
+                 int npts_src, int nt, int nt_big, int nx, int ny) {
+  (void)npts_src;
+  born_handle *h = dflt();
+  if (!h) return record(BORN_ENODEV);
+  if (h->have_space && (n1 != h->n1 || n2 != h->n2 || n3 != h->n3))
+    return record(fail(h, BORN_EINVAL, "rtm_forward: grid mismatch"));
+  if (h->rec.npts != nx * ny || h->rec.nt != nt_big)
+    return record(fail(h, BORN_EINVAL,
+                       "rtm_forward: receiver geometry differs from the "
+                       "transferred one"));
+  if (img) {
+    int rc = born_set_reflectivity(h, img);
+    if (rc) return record(rc);
+  }
+  record(born_rtm_forward(h, jt, nt, dat));
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+"""Seeded synthetic shots for the benchmark and the larger tests.
+
+The reference names no public dataset; these generators stand in with the
+shapes, sizes and value ranges of the benchmark configurations:
+
+* ``c1``: 128^3 model at 10 m, 20-cell boundary -> 176^3 compute grid,
+  nt = 1000, 15 Hz Ricker, 6 flat layers 1500..4000 m/s with a seeded
+  +-3 % smooth perturbation, 64 x 64 receivers at 20 m, 10 m deep.
+* ``c2``: 256^3 model at 10 m, 50-cell boundary -> 368^3, nt = 2000,
+  12 Hz Ricker, layered 1500..4500 m/s with a dipping interface and a
+  Gaussian salt-like blob at 4500 m/s, 128 x 128 receivers at 20 m.
+
+``prepare_shot`` turns a model into the propagator inputs exactly as the
+reference's operator does per shot (rtm_zero_op_3d.cc:139-185 and
+:243-273), using this package's host geometry: compute grid and origin,
+sinc tables, 9-point source with the wavelet's time derivative, receiver
+cells, random-boundary and plain v^2 dt^2 models, and the reflectivity after
+the z first difference.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+SEEDS = dict(velocity=1001, reflectivity=1002, data=1004)
+
+
+def ricker(nt: int, dt: float, f: float, t0: float = 0.064) -> np.ndarray:
+    """util/Wavelet.cc:23-29."""
+    t = -t0 + np.arange(nt) * dt
+    a = (np.pi * f * t) ** 2
+    return ((1 - 2 * a) * np.exp(-a)).astype(np.float32)
+
+
+def _smooth3(a, sigma_cells):
+    # separable Gaussian via FFT along each axis
+    out = a
+    for ax in range(3):
+        n = out.shape[ax]
+        k = np.fft.rfftfreq(n)
+        g = np.exp(-0.5 * (2 * np.pi * k * sigma_cells) ** 2)
+        shape = [1, 1, 1]
+        shape[ax] = g.size
+        out = np.fft.irfft(np.fft.rfft(out, axis=ax) * g.reshape(shape), n=n,
+                           axis=ax)
+    return out
+
+
+def model_c1(n=128, seed=SEEDS["velocity"]):
+    rng = np.random.default_rng(seed)
+    z = np.arange(n)
+    layer = np.minimum(z * 6 // n, 5)
+    v = (1500.0 + 500.0 * layer)[:, None, None] * np.ones((n, n, n))
+    dv = _smooth3(rng.standard_normal((n, n, n)), 4.0)
+    v *= 1 + 0.03 * dv / np.abs(dv).max()
+    return v.astype(np.float32)
+
+
+def model_c2(n=256, seed=SEEDS["velocity"]):
+    rng = np.random.default_rng(seed)
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n),
+                          indexing="ij")
+    v = 1500.0 + 2500.0 * z / (n - 1)
+    dip = np.tan(np.deg2rad(rng.uniform(5, 15)))
+    v = np.where(z > 0.55 * n + dip * (x - n / 2), v + 400.0, v)
+    c = np.array([0.6, 0.5, 0.45]) * n
+    r2 = ((z - c[0]) ** 2 + (y - c[1]) ** 2 + (x - c[2]) ** 2) / (0.1 * n) ** 2
+    blob = np.exp(-r2)
+    v = v * (1 - blob) + 4500.0 * blob
+    return np.clip(v, 1500.0, 4500.0).astype(np.float32)
+
+
+def reflectivity(v, seed=SEEDS["reflectivity"]):
+    """dv/dz normalised to 1, plus seeded sparse +-0.05 spikes."""
+    rng = np.random.default_rng(seed)
+    r = np.zeros_like(v)
+    r[1:] = v[1:] - v[:-1]
+    r /= max(np.abs(r).max(), 1e-30)
+    mask = rng.random(v.shape) < 1e-3
+    r[mask] += rng.choice([-0.05, 0.05], size=int(mask.sum()))
+    return r.astype(np.float32)
+
+
+CONFIGS = {
+    "c1": dict(n=128, d=10.0, nbound=20, nt=1000, f=15.0, model=model_c1,
+               rec=(64, 20.0), src_depth=20.0, rec_depth=10.0),
+    "c2": dict(n=256, d=10.0, nbound=50, nt=2000, f=12.0, model=model_c2,
+               rec=(128, 20.0), src_depth=20.0, rec_depth=10.0),
+}
+
+
+def prepare_shot(born, name: str = "c2", nt: int | None = None,
+                 n: int | None = None, nbound: int | None = None) -> dict:
+    """Propagator inputs for one shot of configuration ``name``."""
+    cfg = dict(CONFIGS[name])
+    if n is not None:
+        cfg["n"] = n
+    if nbound is not None:
+        cfg["nbound"] = nbound
+    n, d, nb = cfg["n"], cfg["d"], cfg["nbound"]
+    vel = cfg["model"](n)
+    dt_data = 0.001
+    nt_data = nt if nt is not None else cfg["nt"]
+    dt, nt_fd = born.calc_stability(float(vel.max()), d, dt_data, nt_data)
+    jt = int(round(dt_data / dt))
+    fat = 4
+    nc = born.compute_size(n, nb, fat)
+    o_c = -d * (nb + fat)
+    o = (o_c, o_c, o_c)
+    dd = (d, d, d)
+    table = born.sinc_table(jt, 8)
+    nt_big = nt_data + 8
+    wav = born.wavelet_deriv(ricker(nt_data, dt_data, cfg["f"]), dt_data)
+    mid = (n // 2) * d
+    locs_s, src = born.source_geometry(mid, mid, cfg["src_depth"], o, dd, nc,
+                                       nc, wav, nt_big)
+    seed = int(locs_s[3] % 10000)
+    shape = (nc, nc, nc)
+    vrand = born.rand_subspace(vel, (0., 0., 0.), dd, float(vel.max()), seed,
+                               (nb, nb, nb), dt, shape, o, dd)
+    vnone = born.rand_subspace(vel, (0., 0., 0.), dd, float(vel.max()), seed,
+                               (0, 0, 0), dt, shape, o, dd)
+    nr, dr = cfg["rec"]
+    r0 = mid - dr * (nr // 2)
+    locs_r = born.receiver_geometry(nr, nr, r0, dr, r0, dr, cfg["rec_depth"],
+                                    o, dd, nc, nc)
+    rng = np.random.default_rng(SEEDS["data"])
+    rec = np.zeros((nr * nr, nt_big), np.float32)
+    rec[:, 4:4 + nt_data] = 1e-3 * rng.standard_normal((nr * nr, nt_data))
+    # model-grid reflectivity -> compute-grid window -> z first difference
+    refl_m = reflectivity(vel)
+    sub = np.zeros(shape, np.float32)
+    born.lib().born_extract_sub(born.fptr(refl_m), n, n, n, born.fptr(sub),
+                                nc, nc, nc, -(nb + fat), -(nb + fat),
+                                -(nb + fat))
+    refl = np.zeros(shape, np.float32)
+    born.lib().born_laplac_forward(0, born.fptr(sub), born.fptr(refl), nc, nc,
+                                   nc)
+    return dict(shape=shape, d=d, nt=nt_fd, jts=jt, jtd=jt, nt_big=nt_big,
+                table_s=table, table_d=table, locs_s=locs_s, src=src,
+                vel1=vrand, vel2=vnone, locs_r=locs_r, rec_nx=nr, rec_ny=nr,
+                rec_in=rec, refl=refl, name=name, model_n=n, nbound=nb)
+
+
+def interior_cells(shape) -> int:
+    nz, ny, nx = shape
+    return (nx - 8) * (ny - 8) * (nz - 8)

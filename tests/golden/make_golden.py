@@ -1,0 +1,53 @@
+"""Generate the golden fixtures for the Born / RTM hot path.
+
+Runs the reference's own CPU propagator (base/cpu_prop.cc and
+base/sinc_bob.cc, compiled from source by ``oracle/Makefile ref``) on small
+seeded cases and stores inputs and outputs in ``tests/golden/*.npz``.  Needs
+the reference sources (present only where the fixtures are made); the
+fixtures themselves travel with the repository.
+
+    python tests/golden/make_golden.py
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+import pyoracle as po  # noqa: E402
+import cases  # noqa: E402
+
+# (name, seed, shape (nz, ny, nx), nt, jt, duplicated receivers)
+CASES = [
+    ("g1_jt1_even", 11, (20, 24, 28), 40, 1, 0),
+    ("g2_jt2_odd", 12, (20, 24, 28), 41, 2, 0),
+    ("g3_jt1_dup", 13, (20, 24, 32), 30, 1, 3),
+]
+
+
+def main():
+    if po.ref_lib() is None:
+        sys.exit("reference sources not available: cannot make fixtures")
+    tabs = {f"sinc_{n}": po.sinc_table(n, 8, ref=True) for n in (1, 2, 3, 4, 8)}
+    np.savez_compressed(os.path.join(HERE, "sinc_tables.npz"), **tabs)
+    for name, seed, shape, nt, jt, dup in CASES:
+        c = cases.make_case(seed, shape=shape, nt=nt, jt=jt,
+                            dup_receivers=dup,
+                            sinc=lambda n: po.sinc_table(n, 8, ref=True))
+        out = po.run_case(po.RefProp(), c)
+        arrays = {k: v for k, v in c.items() if isinstance(v, np.ndarray)}
+        scalars = {k: np.array(v) for k, v in c.items()
+                   if not isinstance(v, np.ndarray)}
+        np.savez_compressed(
+            os.path.join(HERE, f"{name}.npz"),
+            **{f"in_{k}": v for k, v in arrays.items()},
+            **{f"par_{k}": v for k, v in scalars.items()},
+            **{f"out_{k}": v for k, v in out.items()})
+        print(name, {k: float(np.linalg.norm(v)) for k, v in out.items()})
+
+
+if __name__ == "__main__":
+    main()
