@@ -201,7 +201,7 @@ def run_reference_arm(args):
     born = package()
     born.build()
     wl = workload_module()
-    case = wl.prepare_shot(born, args.config)
+    case = wl.prepare_shot(born, args.config, nt=args.nt, n=args.model_n)
     threads = os.cpu_count() or 1
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
@@ -245,7 +245,7 @@ def run_gpu_arm(args):
     born = package()
     born.lib()
     wl = workload_module()
-    case = wl.prepare_shot(born, args.config)
+    case = wl.prepare_shot(born, args.config, nt=args.nt, n=args.model_n)
     nz, ny, nx = case["shape"]
     nt, jt = case["nt"], case["jts"]
     n_int = wl.interior_cells(case["shape"])
@@ -442,6 +442,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--model-n", type=int, default=None,
+                    help="smaller model edge (profiling cases)")
+    ap.add_argument("--nt", type=int, default=None,
+                    help="fewer time steps (profiling cases)")
     ap.add_argument("--tile", type=int, default=-1)
     ap.add_argument("--zseg", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=2)
