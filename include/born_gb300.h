@@ -145,6 +145,21 @@ int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
 int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap, float *img);
 int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out);
 
+/* Nonlinear modelling through vel2 with the taper (the background of
+ * rtmForward, cpu_prop.cc:36-45): traces accumulate into the device traces
+ * of born_set_receiver_func (copied to traces_out when non-null). */
+int born_model(born_handle *h, int jt, int nt, float *traces_out);
+/* Exact linearised Born forward: derivative of born_model with respect to
+ * vel2 (v^2 dt^2) along the perturbation given by born_set_reflectivity.
+ * Traces accumulate into the device traces. */
+int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out);
+/* Exact adjoint of born_lin_forward: reads the device traces, returns the
+ * model-space gradient (n1*n2*n3) in model_out (also left in the device
+ * image).  The background is checkpointed every `interval` steps (two levels
+ * per checkpoint) and recomputed segment by segment. */
+int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
+                     float *model_out);
+
 /* Device results and state transfers (host arrays of n1*n2*n3 floats, or
  * npts*nt_big for traces) */
 int born_get_image(born_handle *h, float *img_out);

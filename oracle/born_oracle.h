@@ -92,6 +92,15 @@ void oracle_rtm_adjointf(oracle_propf *s, float *src_p0, float *src_p1,
 void oracle_rtm_forwardf(oracle_propf *s, int jt, const float *img,
                          float *rec, int nt);
 
+/* nonlinear modelling and its exact linearisation (no reference
+ * counterpart; built from the same primitives, see oracle_prop_impl.h) */
+void oracle_modelf(oracle_propf *s, int jt, float *rec, int nt);
+void oracle_lin_forwardf(oracle_propf *s, int jt, const float *m, float *rec,
+                         int nt);
+void oracle_modeld(oracle_propd *s, int jt, double *rec, int nt);
+void oracle_lin_forwardd(oracle_propd *s, int jt, const double *m,
+                         double *rec, int nt);
+
 /* ---- double (accuracy) oracle ---- */
 void oracle_source_propd(oracle_propd *s, double *p0, double *p1, int jts,
                          int nt);

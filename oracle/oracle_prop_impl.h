@@ -224,6 +224,94 @@ void FN(oracle_rtm_forward)(PROPT *s, int jt, const REAL *img, REAL *rec,
   free(b3);
 }
 
+/* A p (the stencil sum of cpuProp::prop without the velocity factor) over
+ * the interior, in the same summation order; exterior cells are left 0. */
+static void FN(oracle_stencil_sum)(const PROPT *s, const REAL *p1, REAL *out) {
+  const int nx = s->nx, ny = s->ny, nz = s->nz;
+  const long long n12 = (long long)nx * ny;
+  const REAL *c = s->coeffs;
+#pragma omp parallel for schedule(static)
+  for (int i3 = 4; i3 < nz - 4; i3++) {
+    for (int i2 = 4; i2 < ny - 4; i2++) {
+      long long ii = (long long)i2 * nx + 4 + n12 * i3;
+      for (int i1 = 4; i1 < nx - 4; i1++, ii++) {
+        out[ii] = c[K_C0] * p1[ii] + c[K_CX1] * (p1[ii - 1] + p1[ii + 1]) +
+                  c[K_CX2] * (p1[ii - 2] + p1[ii + 2]) +
+                  c[K_CX3] * (p1[ii - 3] + p1[ii + 3]) +
+                  c[K_CX4] * (p1[ii - 4] + p1[ii + 4]) +
+                  c[K_CY1] * (p1[ii - nx] + p1[ii + nx]) +
+                  c[K_CY2] * (p1[ii - 2 * nx] + p1[ii + 2 * nx]) +
+                  c[K_CY3] * (p1[ii - 3 * nx] + p1[ii + 3 * nx]) +
+                  c[K_CY4] * (p1[ii - 4 * nx] + p1[ii + 4 * nx]) +
+                  c[K_CZ1] * (p1[ii - n12] + p1[ii + n12]) +
+                  c[K_CZ2] * (p1[ii - 2 * n12] + p1[ii + 2 * n12]) +
+                  c[K_CZ3] * (p1[ii - 3 * n12] + p1[ii + 3 * n12]) +
+                  c[K_CZ4] * (p1[ii - 4 * n12] + p1[ii + 4 * n12]);
+      }
+    }
+  }
+}
+
+/* Nonlinear modelling: the background field of cpuProp::rtmForward
+ * (cpu_prop.cc:36-41: vel2, taper, source at +1/jt) with the receiver
+ * traces sampled from it as dataExtract does from r (cpu_prop.cc:45). */
+void FN(oracle_model)(PROPT *s, int jt, REAL *rec, int nt) {
+  s->jt = jt;
+  s->rec = rec;
+  s->dir = 1;
+  REAL *b0 = (REAL *)calloc((size_t)s->n123, sizeof(REAL));
+  REAL *b1 = (REAL *)calloc((size_t)s->n123, sizeof(REAL));
+  REAL *p0 = b0, *p1 = b1;
+  for (int it = 0; it < nt; it++) {
+    int id = it / jt, ii = it - id * jt;
+    FN(oracle_prop_step)(s, p0, p1, s->vel2);
+    FN(oracle_damp)(s, p0, p1);
+    FN(oracle_inject_source)(s, id, ii, p0);
+    FN(oracle_data_extract)(s, id, ii, p0);
+    REAL *pt = p0;
+    p0 = p1;
+    p1 = pt;
+  }
+  free(b0);
+  free(b1);
+}
+
+/* Exact linearisation of oracle_model with respect to vel2 along m:
+ * r_{t+1} = B (vel2 A r_t + 2 r_t - B r_{t-1} + m (A s_t)), traces from r. */
+void FN(oracle_lin_forward)(PROPT *s, int jt, const REAL *m, REAL *rec,
+                            int nt) {
+  s->jt = jt;
+  s->rec = rec;
+  s->dir = 1;
+  const size_t n = (size_t)s->n123;
+  REAL *b0 = (REAL *)calloc(n, sizeof(REAL)), *b1 = (REAL *)calloc(n, sizeof(REAL));
+  REAL *b2 = (REAL *)calloc(n, sizeof(REAL)), *b3 = (REAL *)calloc(n, sizeof(REAL));
+  REAL *g = (REAL *)calloc(n, sizeof(REAL));
+  REAL *s_p0 = b0, *s_p1 = b1, *r_p0 = b2, *r_p1 = b3;
+  for (int it = 0; it < nt; it++) {
+    int id = it / jt, ii = it - id * jt;
+    FN(oracle_stencil_sum)(s, s_p1, g);
+    FN(oracle_prop_step)(s, s_p0, s_p1, s->vel2);
+    FN(oracle_prop_step)(s, r_p0, r_p1, s->vel2);
+    for (size_t i = 0; i < n; i++) r_p0[i] = r_p0[i] + m[i] * g[i];
+    FN(oracle_damp)(s, s_p0, s_p1);
+    FN(oracle_damp)(s, r_p0, r_p1);
+    FN(oracle_inject_source)(s, id, ii, s_p0);
+    FN(oracle_data_extract)(s, id, ii, r_p0);
+    REAL *pt = s_p0;
+    s_p0 = s_p1;
+    s_p1 = pt;
+    pt = r_p0;
+    r_p0 = r_p1;
+    r_p1 = pt;
+  }
+  free(b0);
+  free(b1);
+  free(b2);
+  free(b3);
+  free(g);
+}
+
 #undef FN
 #undef PROPT
 #undef CAT

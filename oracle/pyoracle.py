@@ -124,6 +124,10 @@ def port_lib():
             "oracle_rtm_adjointd": (None, [PD, _dp, _dp, _dp, C.c_int,
                                            C.c_int]),
             "oracle_rtm_forwardd": (None, [PD, C.c_int, _dp, _dp, C.c_int]),
+            "oracle_modelf": (None, [P, C.c_int, _fp, C.c_int]),
+            "oracle_lin_forwardf": (None, [P, C.c_int, _fp, _fp, C.c_int]),
+            "oracle_modeld": (None, [PD, C.c_int, _dp, C.c_int]),
+            "oracle_lin_forwardd": (None, [PD, C.c_int, _dp, _dp, C.c_int]),
             "oracle_sinc_table": (None, [C.c_int, C.c_int, _fp]),
             "oracle_calc_stability": (C.c_float, [C.c_float, C.c_float,
                                                   C.c_float, C.c_int, _ip]),
@@ -282,6 +286,18 @@ class PortProp:
         self.lib.oracle_rtm_forwardf(C.byref(self.s), jt, fptr(img),
                                      fptr(rec), nt)
 
+    def model(self, jt, rec, nt):
+        """Nonlinear modelling (background of rtmForward, traces from s)."""
+        self._keep["rec"] = rec
+        self.lib.oracle_modelf(C.byref(self.s), jt, fptr(rec), nt)
+
+    def lin_forward(self, jt, m, rec, nt):
+        """Exact linearised Born forward along m (= perturbation of vel2)."""
+        m = self._keep["m"] = self._arr(m)
+        self._keep["rec"] = rec
+        self.lib.oracle_lin_forwardf(C.byref(self.s), jt, fptr(m), fptr(rec),
+                                     nt)
+
     # primitives, for unit tests
     def prop(self, p0, p1, vel):
         self.lib.oracle_prop_stepf(C.byref(self.s), fptr(p0), fptr(p1),
@@ -323,6 +339,16 @@ class PortProp64(PortProp):
                    rec_ny):
         self.lib.oracle_rtm_forwardd(C.byref(self.s), jt, dptr(img),
                                      dptr(rec), nt)
+
+    def model(self, jt, rec, nt):
+        self._keep["rec"] = rec
+        self.lib.oracle_modeld(C.byref(self.s), jt, dptr(rec), nt)
+
+    def lin_forward(self, jt, m, rec, nt):
+        m = self._keep["m"] = self._arr(m)
+        self._keep["rec"] = rec
+        self.lib.oracle_lin_forwardd(C.byref(self.s), jt, dptr(m), dptr(rec),
+                                     nt)
 
 
 class RefProp:
@@ -418,6 +444,8 @@ def run_case(prop, case: dict, which: str = "all") -> dict:
     prop.transferVelFunc1(nx, ny, nz, case["vel1"])
     prop.transferVelFunc2(nx, ny, nz, case["vel2"])
     nt = case["nt"]
+    if which == "none":
+        return out
     if which in ("all", "adjoint", "source"):
         rec = np.ascontiguousarray(case["rec_in"], dtype=dt)
         prop.transferReceiverFunc(case["rec_nx"], case["rec_ny"],

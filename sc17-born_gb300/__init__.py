@@ -70,6 +70,9 @@ _SIGS = {
     "born_source_prop": (C.c_int, [_vp, C.c_int, C.c_int, _fp, _fp]),
     "born_rtm_adjoint": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _fp]),
     "born_rtm_forward": (C.c_int, [_vp, C.c_int, C.c_int, _fp]),
+    "born_model": (C.c_int, [_vp, C.c_int, C.c_int, _fp]),
+    "born_lin_forward": (C.c_int, [_vp, C.c_int, C.c_int, _fp]),
+    "born_lin_adjoint": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _fp]),
     "born_get_image": (C.c_int, [_vp, _fp]),
     "born_get_traces": (C.c_int, [_vp, _fp]),
     "born_get_source_levels": (C.c_int, [_vp, _fp, _fp]),
@@ -258,6 +261,8 @@ class Gb300Prop(Handle):
         l = np.ascontiguousarray(locs, np.int32)
         assert rec.dtype == np.float32 and rec.flags.c_contiguous
         self._rec = rec
+        self._rec_nx, self._rec_ny, self._rec_nt = nx, ny, nt
+        self._rec_locs = l
         self.check(self.lib.born_set_receiver_func(self.h, nx, ny, nt, iptr(l),
                                                    fptr(rec)))
 
@@ -298,6 +303,35 @@ class Gb300Prop(Handle):
 
     def rtm_forward_device(self, jt, nt):
         self.check(self.lib.born_rtm_forward(self.h, jt, nt, None))
+
+    # ---- nonlinear modelling and the exact linearised Born pair ----
+    def set_traces(self, traces):
+        """Replace the device traces (same receivers, same nt)."""
+        self.transferReceiverFunc(self._rec_nx, self._rec_ny, self._rec_nt,
+                                  self._rec_locs, f32(traces))
+
+    def model(self, jt, nt):
+        """Nonlinear modelling through vel2; returns the traces."""
+        out = np.zeros_like(self._rec)
+        self.zero_traces()
+        self.check(self.lib.born_model(self.h, jt, nt, fptr(out)))
+        return out
+
+    def lin_forward(self, jt, nt, m):
+        """Exact linearised Born forward along m (perturbation of vel2)."""
+        self.check(self.lib.born_set_reflectivity(self.h, fptr(f32(m))))
+        out = np.zeros_like(self._rec)
+        self.zero_traces()
+        self.check(self.lib.born_lin_forward(self.h, jt, nt, fptr(out)))
+        return out
+
+    def lin_adjoint(self, jt, nt, traces, interval=50):
+        """Exact adjoint of lin_forward applied to traces."""
+        self.set_traces(traces)
+        out = np.zeros(self.shape, np.float32)
+        self.check(self.lib.born_lin_adjoint(self.h, jt, nt, interval,
+                                             fptr(out)))
+        return out
 
     def get_image(self):
         out = np.empty(self.shape, np.float32)

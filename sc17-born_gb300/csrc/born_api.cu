@@ -99,7 +99,12 @@ struct born_handle {
   int tile_cfg = -1, zseg = 0;
   long long launches = 0;
   int ntblock = 0;
+  // TMA descriptors by (buffer, tile config * 2 + kind); kind 0 = halo box,
+  // 1 = centre tile
   std::map<std::pair<const void *, int>, CUtensorMap> maps;
+  // exact linearised adjoint: checkpoints and the per-segment A s buffer
+  float *ckpt = nullptr, *gbuf = nullptr;
+  size_t ckpt_levels = 0, gbuf_levels = 0;
 };
 
 namespace {
@@ -131,6 +136,10 @@ void free_fields(born_handle *h) {
     cudaFree(*b);
     *b = nullptr;
   }
+  cudaFree(h->ckpt);
+  cudaFree(h->gbuf);
+  h->ckpt = h->gbuf = nullptr;
+  h->ckpt_levels = h->gbuf_levels = 0;
   h->maps.clear();
   h->have_space = h->have_vel1 = h->have_vel2 = h->have_refl = false;
   h->src_levels_valid = false;
@@ -229,8 +238,9 @@ int upload_points(born_handle *h, DevPoints &dp, int npts, int nt,
   return BORN_OK;
 }
 
-int get_map(born_handle *h, const float *buf, int cfg, CUtensorMap *out) {
-  auto key = std::make_pair((const void *)buf, cfg);
+int get_map(born_handle *h, const float *buf, int cfg, int kind,
+            CUtensorMap *out) {
+  auto key = std::make_pair((const void *)buf, cfg * 2 + kind);
   auto it = h->maps.find(key);
   if (it != h->maps.end()) {
     *out = it->second;
@@ -245,7 +255,9 @@ int get_map(born_handle *h, const float *buf, int cfg, CUtensorMap *out) {
                               (cuuint64_t)h->n3};
   const cuuint64_t strides[2] = {(cuuint64_t)h->n1 * 4,
                                  (cuuint64_t)h->n1 * h->n2 * 4};
-  const cuuint32_t box[3] = {(cuuint32_t)(tx + 8), (cuuint32_t)(ty + 8), 1};
+  const int halo = kind == 0 ? 2 * born::kRadius : 0;
+  const cuuint32_t box[3] = {(cuuint32_t)(tx + halo), (cuuint32_t)(ty + halo),
+                             1};
   const cuuint32_t estr[3] = {1, 1, 1};
   CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)buf, dims,
                    strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -258,11 +270,11 @@ int get_map(born_handle *h, const float *buf, int cfg, CUtensorMap *out) {
   return BORN_OK;
 }
 
-// Tiling: the configured one, else 64x16 tiles; z segments sized so that
+// Tiling: the configured one, else 32x16 tiles; z segments sized so that
 // the grid covers every SM a few times.
-void pick_tiling(born_handle *h, int nfields, int *cfg, int *zseg, int *tiles_x,
-                 int *tiles_y) {
-  int c = h->tile_cfg >= 0 ? h->tile_cfg : 0;
+void pick_tiling(born_handle *h, int mode, bool pa, bool pb, int *cfg,
+                 int *zseg, int *tiles_x, int *tiles_y) {
+  int c = h->tile_cfg >= 0 ? h->tile_cfg : 1;
   int tx, ty;
   born::tile_cfg_dims(c, &tx, &ty);
   *cfg = c;
@@ -275,7 +287,7 @@ void pick_tiling(born_handle *h, int nfields, int *cfg, int *zseg, int *tiles_x,
   }
   int sms = 148;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-  const size_t smem = born::step_smem_bytes(c, std::max(1, nfields));
+  const size_t smem = born::step_smem_bytes(c, mode, pa, pb);
   int per_sm = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
   per_sm = std::min(per_sm, 2048 / ((tx / 4) * ty));
   const long long target = 2ll * sms * per_sm;
@@ -314,20 +326,29 @@ void base_params(born_handle *h, StepParams &p) {
   p.err = h->err_dev;
 }
 
+// One step launch.  a_cur / b_cur: current levels of the propagated fields
+// (halo boxes); centre[slot]: the per-cell inputs by born::CentreSlot.
 int launch(born_handle *h, int mode, bool pa, bool pb, const float *a_cur,
-           const float *b_cur, StepParams &p) {
-  const int nf = (pa ? 1 : 0) + (pb ? 1 : 0);
+           const float *b_cur, const float *const centre[born::kNumCentre],
+           StepParams &p) {
   int cfg, zseg, tx, ty;
-  pick_tiling(h, nf, &cfg, &zseg, &tx, &ty);
+  pick_tiling(h, mode, pa, pb, &cfg, &zseg, &tx, &ty);
   p.tiles_x = tx;
   p.tiles_y = ty;
   p.zseg = zseg;
-  CUtensorMap ma, mb;
-  int rc = get_map(h, pa ? a_cur : (b_cur ? b_cur : h->s0), cfg, &ma);
+  born::StepMaps maps;
+  const float *any = h->vel2;  // any valid grid buffer for unused slots
+  int rc = get_map(h, a_cur ? a_cur : any, cfg, 0, &maps.box_a);
+  if (!rc) rc = get_map(h, b_cur ? b_cur : any, cfg, 0, &maps.box_b);
+  const unsigned mask = born::centre_mask(mode, pa, pb);
+  for (int sl = 0; sl < born::kNumCentre && !rc; ++sl) {
+    const bool used = mask & (1u << sl);
+    if (used && !centre[sl])
+      return fail(h, BORN_ESTATE, "step input %d missing", sl);
+    rc = get_map(h, used ? centre[sl] : any, cfg, 1, &maps.cm[sl]);
+  }
   if (rc) return rc;
-  rc = get_map(h, pb ? b_cur : (a_cur ? a_cur : h->s0), cfg, &mb);
-  if (rc) return rc;
-  CK(h, born::launch_step(mode, pa, pb, cfg, ma, mb, p, h->stream));
+  CK(h, born::launch_step(mode, pa, pb, cfg, maps, p, h->stream));
   h->launches++;
   return BORN_OK;
 }
@@ -531,12 +552,12 @@ int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
     const int id = it / h->jt_s, ii = it - id * h->jt_s;
     StepParams p;
     base_params(h, p);
-    p.a_cur = p1;
-    p.a_old = p0;
-    p.a_vel = h->vel1;
+    p.a_out = p0;
     p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
     p.pb = point_view(h->src, 0, 0, h->tab_s, 0.f, false);
-    rc = launch(h, kModeSource, true, false, p1, nullptr, p);
+    const float *cen[born::kNumCentre] = {p0, nullptr, h->vel1, nullptr,
+                                          nullptr};
+    rc = launch(h, kModeSource, true, false, p1, nullptr, cen, p);
     if (!rc) rc = poll_error(h, it);
     if (rc) return rc;
     std::swap(p0, p1);
@@ -582,16 +603,14 @@ int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap,
     const bool pa = it > 0, pb = it < nt - 1;
     StepParams p;
     base_params(h, p);
-    p.a_cur = rp1;
-    p.a_old = rp0;
-    p.a_vel = h->vel2;
-    p.b_cur = sp1;
-    p.b_old = sp0;
-    p.b_vel = h->vel1;
-    p.img = h->img;
+    p.a_out = rp0;
+    p.b_out = sp0;
+    p.img_out = h->img;
     p.pa = point_view(h->rec, id, ii, h->tab_d, scale, true);
     p.pb = pending;
-    rc = launch(h, kModeAdjoint, pa, pb, rp1, sp1, p);
+    const float *cen[born::kNumCentre] = {rp0, sp0, h->vel2, h->vel1, h->img};
+    rc = launch(h, kModeAdjoint, pa, pb, pa ? rp1 : nullptr,
+                pb ? sp1 : nullptr, cen, p);
     if (!rc) rc = poll_error(h, nt - 1 - it);
     if (rc) return rc;
     // the source injection of this step goes into the current level, which
@@ -633,16 +652,13 @@ int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out) {
     const int id = it / jt, ii = it - id * jt;
     StepParams p;
     base_params(h, p);
-    p.a_cur = sp1;
-    p.a_old = sp0;
-    p.a_vel = h->vel2;
-    p.b_cur = rp1;
-    p.b_old = rp0;
-    p.b_vel = h->vel2;
-    p.img = h->refl;
+    p.a_out = sp0;
+    p.b_out = rp0;
     p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
     p.pb = point_view(h->rec, id, ii, h->tab_d, 0.f, true);
-    rc = launch(h, kModeForward, true, true, sp1, rp1, p);
+    const float *cen[born::kNumCentre] = {sp0, rp0, h->vel2, nullptr,
+                                          h->refl};
+    rc = launch(h, kModeForward, true, true, sp1, rp1, cen, p);
     if (!rc) rc = poll_error(h, it);
     if (rc) return rc;
     std::swap(sp0, sp1);
@@ -652,6 +668,196 @@ int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out) {
     CK(h, cudaMemcpyAsync(traces_out, h->rec.traces,
                           (size_t)h->rec.npts * h->rec.nt * 4,
                           cudaMemcpyDeviceToHost, h->stream));
+    return check_device_error(h);
+  }
+  return BORN_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Nonlinear modelling and the exact linearised Born pair.
+//
+// Modelling (the background of cpuProp::rtmForward with its own traces):
+//   s_{t+1} = B (V A s_t + 2 s_t - B s_{t-1}) + Q_t,   d_t = E_t s_{t+1}
+// with V = vel2 (v^2 dt^2), B the taper, Q_t the source injection and E_t
+// the sinc extraction of step t.  Its derivative with respect to V along m:
+//   r_{t+1} = B (V A r_t + 2 r_t - B r_{t-1} + m (A s_t)),   δd_t = E_t r_{t+1}
+// and the exact transpose of that map, in the variable w = V μ:
+//   w_{t+1} = B (V A w_{t+2} + 2 w_{t+2} - B w_{t+3} + V E_t^T δd),
+//   m̄ = (1/V) Σ_t (A s_t) w_{t+1}
+// (A is the symmetric interior stencil, V and B are diagonal).  The adjoint
+// needs A s_t in reverse order: s is checkpointed every `interval` steps and
+// each segment is recomputed forward, storing A s_t, before the reverse
+// sweep over it.
+
+int born_model(born_handle *h, int jt, int nt, float *traces_out) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (nt < 0 || jt < 1) return fail(h, BORN_EINVAL, "nt < 0 or jt < 1");
+  if (!h->have_vel2) return fail(h, BORN_ESTATE, "vel2 not transferred");
+  if (jt > h->jt_s || jt > h->jt_d)
+    return fail(h, BORN_EINVAL, "jt %d exceeds the sinc tables' rows", jt);
+  const size_t bytes = (size_t)h->n123 * 4;
+  CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
+  float *sp0 = h->f0, *sp1 = h->f1;
+  const float scale = 1 / (float)jt;
+  for (int it = 0; it < nt; ++it) {
+    const int id = it / jt, ii = it - id * jt;
+    StepParams p;
+    base_params(h, p);
+    p.a_out = sp0;
+    p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
+    p.pb = point_view(h->rec, id, ii, h->tab_d, 0.f, true);
+    const float *cen[born::kNumCentre] = {sp0, nullptr, h->vel2, nullptr,
+                                          nullptr};
+    rc = launch(h, born::kModeModel, true, false, sp1, nullptr, cen, p);
+    if (!rc) rc = poll_error(h, it);
+    if (rc) return rc;
+    std::swap(sp0, sp1);
+  }
+  if (traces_out) {
+    CK(h, cudaMemcpyAsync(traces_out, h->rec.traces,
+                          (size_t)h->rec.npts * h->rec.nt * 4,
+                          cudaMemcpyDeviceToHost, h->stream));
+    return check_device_error(h);
+  }
+  return BORN_OK;
+}
+
+int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (nt < 0 || jt < 1) return fail(h, BORN_EINVAL, "nt < 0 or jt < 1");
+  if (!h->have_vel2 || !h->have_refl)
+    return fail(h, BORN_ESTATE, "vel2 or model perturbation not transferred");
+  if (jt > h->jt_s || jt > h->jt_d)
+    return fail(h, BORN_EINVAL, "jt %d exceeds the sinc tables' rows", jt);
+  const size_t bytes = (size_t)h->n123 * 4;
+  CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->r0, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->r1, 0, bytes, h->stream));
+  float *sp0 = h->f0, *sp1 = h->f1, *rp0 = h->r0, *rp1 = h->r1;
+  const float scale = 1 / (float)jt;
+  for (int it = 0; it < nt; ++it) {
+    const int id = it / jt, ii = it - id * jt;
+    StepParams p;
+    base_params(h, p);
+    p.a_out = sp0;
+    p.b_out = rp0;
+    p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
+    p.pb = point_view(h->rec, id, ii, h->tab_d, 0.f, true);
+    const float *cen[born::kNumCentre] = {sp0, rp0, h->vel2, nullptr,
+                                          h->refl};
+    rc = launch(h, born::kModeBornLin, true, true, sp1, rp1, cen, p);
+    if (!rc) rc = poll_error(h, it);
+    if (rc) return rc;
+    std::swap(sp0, sp1);
+    std::swap(rp0, rp1);
+  }
+  if (traces_out) {
+    CK(h, cudaMemcpyAsync(traces_out, h->rec.traces,
+                          (size_t)h->rec.npts * h->rec.nt * 4,
+                          cudaMemcpyDeviceToHost, h->stream));
+    return check_device_error(h);
+  }
+  return BORN_OK;
+}
+
+namespace {
+int ensure_levels(born_handle *h, float **buf, size_t *have, size_t levels) {
+  if (*have >= levels) return BORN_OK;
+  cudaFree(*buf);
+  *buf = nullptr;
+  *have = 0;
+  CK(h, cudaMalloc(buf, levels * (size_t)h->n123 * 4));
+  *have = levels;
+  return BORN_OK;
+}
+}  // namespace
+
+int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
+                     float *model_out) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (nt < 1 || jt < 1 || interval < 1)
+    return fail(h, BORN_EINVAL, "nt, jt and interval must be >= 1");
+  if (!h->have_vel2) return fail(h, BORN_ESTATE, "vel2 not transferred");
+  if (jt > h->jt_s || jt > h->jt_d)
+    return fail(h, BORN_EINVAL, "jt %d exceeds the sinc tables' rows", jt);
+  const size_t n = (size_t)h->n123, bytes = n * 4;
+  const int nseg = (nt + interval - 1) / interval;
+  rc = ensure_levels(h, &h->ckpt, &h->ckpt_levels, 2 * (size_t)nseg);
+  if (!rc) rc = ensure_levels(h, &h->gbuf, &h->gbuf_levels, (size_t)interval);
+  if (rc) return rc;
+  const float scale = 1 / (float)jt;
+  auto model_step = [&](float *sp0, float *sp1, int it, float *g) {
+    const int id = it / jt, ii = it - id * jt;
+    StepParams p;
+    base_params(h, p);
+    p.a_out = sp0;
+    p.g_out = g;
+    p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
+    p.pb = point_view(h->rec, id, ii, h->tab_d, 0.f, false);
+    const float *cen[born::kNumCentre] = {sp0, nullptr, h->vel2, nullptr,
+                                          nullptr};
+    return launch(h, born::kModeModel, true, false, sp1, nullptr, cen, p);
+  };
+  // forward sweep of the background, checkpointing (old, cur) per segment
+  CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
+  float *sp0 = h->f0, *sp1 = h->f1;
+  for (int it = 0; it < nt; ++it) {
+    if (it % interval == 0) {
+      float *ck = h->ckpt + 2 * (size_t)(it / interval) * n;
+      CK(h, cudaMemcpyAsync(ck, sp0, bytes, cudaMemcpyDeviceToDevice, h->stream));
+      CK(h, cudaMemcpyAsync(ck + n, sp1, bytes, cudaMemcpyDeviceToDevice,
+                            h->stream));
+    }
+    rc = model_step(sp0, sp1, it, nullptr);
+    if (!rc) rc = poll_error(h, it);
+    if (rc) return rc;
+    std::swap(sp0, sp1);
+  }
+  // reverse sweep
+  CK(h, cudaMemsetAsync(h->r0, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->r1, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->img, 0, bytes, h->stream));
+  float *wp0 = h->r0, *wp1 = h->r1;
+  int steps = 0;
+  for (int seg = nseg - 1; seg >= 0; --seg) {
+    const int t0 = seg * interval, t1 = std::min(nt, t0 + interval);
+    const float *ck = h->ckpt + 2 * (size_t)seg * n;
+    float *a0 = h->f0, *a1 = h->f1;
+    CK(h, cudaMemcpyAsync(a0, ck, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(a1, ck + n, bytes, cudaMemcpyDeviceToDevice,
+                          h->stream));
+    for (int it = t0; it < t1; ++it) {
+      rc = model_step(a0, a1, it, h->gbuf + (size_t)(it - t0) * n);
+      if (!rc) rc = poll_error(h, steps++);
+      if (rc) return rc;
+      std::swap(a0, a1);
+    }
+    for (int it = t1 - 1; it >= t0; --it) {
+      const int id = it / jt, ii = it - id * jt;
+      StepParams p;
+      base_params(h, p);
+      p.a_out = wp0;
+      p.img_out = h->img;
+      p.pa = point_view(h->rec, id, ii, h->tab_d, 1.f, true);
+      const float *g = h->gbuf + (size_t)(it - t0) * n;
+      const float *cen[born::kNumCentre] = {wp0, g, h->vel2, nullptr, h->img};
+      rc = launch(h, born::kModeBornAdj, true, false, wp1, nullptr, cen, p);
+      if (!rc) rc = poll_error(h, steps++);
+      if (rc) return rc;
+      std::swap(wp0, wp1);
+    }
+  }
+  CK(h, born::launch_divide(h->img, h->vel2, h->img, h->n123, h->stream));
+  h->launches++;
+  if (model_out) {
+    CK(h, cudaMemcpyAsync(model_out, h->img, bytes, cudaMemcpyDeviceToHost,
+                          h->stream));
     return check_device_error(h);
   }
   return BORN_OK;

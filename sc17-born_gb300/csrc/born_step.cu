@@ -1,4 +1,6 @@
 // Fused 2.5D time-step kernels (see born_step.cuh for the design).
+#include <algorithm>
+
 #include "born_step.cuh"
 
 namespace born {
@@ -168,12 +170,6 @@ __device__ __forceinline__ void extract_row(const PointSet &ps, int n1, int n2,
   }
 }
 
-__device__ __forceinline__ float4 ld4(const float *p) {
-  return *reinterpret_cast<const float4 *>(p);
-}
-__device__ __forceinline__ float4 ldg4(const float *p) {
-  return __ldg(reinterpret_cast<const float4 *>(p));
-}
 __device__ __forceinline__ void st4(float *p, const float4 &v) {
   *reinterpret_cast<float4 *>(p) = v;
 }
@@ -197,24 +193,62 @@ __device__ __forceinline__ void gather(const float *box, int brow, int bcol,
 }
 
 // ---------------------------------------------------------------------------
+// Compile-time description of a mode
+
+template <int MODE, bool PA, bool PB>
+struct ModeTraits {
+  static constexpr bool kTwoField = (MODE == kModeForward ||
+                                     MODE == kModeBornLin ||
+                                     MODE == kModeAdjoint);
+  static constexpr bool kBoxA = PA;
+  static constexpr bool kBoxB = kTwoField && PB;
+  static constexpr int kNF = (kBoxA ? 1 : 0) + (kBoxB ? 1 : 0);
+  static constexpr unsigned kMask =
+      MODE == kModeSource || MODE == kModeModel
+          ? (1u << kOldA) | (1u << kVelA)
+      : MODE == kModeForward || MODE == kModeBornLin
+          ? (1u << kOldA) | (1u << kOldB) | (1u << kVelA) | (1u << kImg)
+      : MODE == kModeAdjoint
+          ? (1u << kOldA) | (1u << kOldB) | (1u << kImg) |
+                (PA ? (1u << kVelA) : 0u) | (PB ? (1u << kVelB) : 0u)
+          : /* kModeBornAdj: OldB slot carries g = A s */
+          (1u << kOldA) | (1u << kOldB) | (1u << kVelA) | (1u << kImg);
+  static constexpr int kNC = __builtin_popcount(kMask);
+  // tile index of a slot inside a centre stage
+  __host__ __device__ static constexpr int pos(int slot) {
+    return __builtin_popcount(kMask & ((1u << slot) - 1u));
+  }
+  static constexpr bool kDampA = MODE != kModeSource;
+  static constexpr bool kDampB = MODE == kModeForward || MODE == kModeBornLin;
+};
+
+template <int TX, int TY>
+struct Tile {
+  static constexpr int kBX = TX + 2 * kRadius, kBY = TY + 2 * kRadius;
+  static constexpr int kBoxFloats = kBX * kBY;
+  static constexpr int kBoxPitch = ((kBoxFloats * 4 + 127) / 128) * 32;
+  static constexpr int kCFloats = TX * TY;
+  static constexpr int kThreads = (TX / 4) * TY;
+};
+
 template <int MODE, bool PA, bool PB, int TX, int TY>
-__global__ void __launch_bounds__(TileShape<TX, TY>::kThreads)
-    step_kernel(const __grid_constant__ CUtensorMap tm_a,
-                const __grid_constant__ CUtensorMap tm_b,
-                const StepParams p) {
-  using T = TileShape<TX, TY>;
-  constexpr int NF = (PA ? 1 : 0) + (PB ? 1 : 0);
-  constexpr int BX = T::kBX;
-  constexpr int PITCH = T::kBoxPitch;
+__global__ void __launch_bounds__(Tile<TX, TY>::kThreads)
+    step_kernel(const __grid_constant__ StepMaps maps, const StepParams p) {
+  using M = ModeTraits<MODE, PA, PB>;
+  using T = Tile<TX, TY>;
+  constexpr int NF = M::kNF, NC = M::kNC;
+  constexpr int BX = T::kBX, PITCH = T::kBoxPitch, CF = T::kCFloats;
   constexpr uint32_t kBoxBytes = T::kBoxFloats * 4u;
+  constexpr uint32_t kCBytes = T::kCFloats * 4u;
   extern __shared__ __align__(128) float smem_raw[];
   __shared__ __align__(8) uint64_t bars[kStages];
+  __shared__ __align__(8) uint64_t cbars[kCStages];
   __shared__ int abort_flag;
   __shared__ float s_bound[kNBound];
   // TMA destinations need 128-byte alignment: align the dynamic base here
   // (the launch reserves 128 spare bytes for this)
   float *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u) / 4u;
-
+  float *cring = smem + kStages * NF * PITCH;
 
   const int tid = threadIdx.x;
   const int lx = tid % (TX / 4), ly = tid / (TX / 4);
@@ -234,12 +268,12 @@ __global__ void __launch_bounds__(TileShape<TX, TY>::kThreads)
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int x = gx + j;
-    const int ex = min(x - 4, n1 - 4 - x), ey = min(gy - 4, n2 - 4 - gy);
-    exy[j] = min(ex, ey);
+    exy[j] = min(min(x - 4, n1 - 4 - x), min(gy - 4, n2 - 4 - gy));
   }
 
   if (tid == 0) {
     for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < kCStages; ++s) mbar_init(&cbars[s], 1);
     // a wait elsewhere already gave up: the whole CTA leaves untouched
     abort_flag = *reinterpret_cast<volatile unsigned int *>(p.err) != 0u;
     mbar_fence_init();
@@ -248,20 +282,34 @@ __global__ void __launch_bounds__(TileShape<TX, TY>::kThreads)
   __syncthreads();
   if (abort_flag) return;  // uniform: read after the barrier
 
-  const int K = (z1 - z0) + 2 * kRadius;  // planes z0-4 .. z1+3
-  auto issue = [&](int k) {
+  const int K = (z1 - z0) + 2 * kRadius;  // box planes z0-4 .. z1+3
+  const int J = z1 - z0;                  // output planes
+  auto issue_box = [&](int k) {
     const int plane = z0 - kRadius + k;
     const int st = k % kStages;
     mbar_expect_tx(&bars[st], NF * kBoxBytes);
     float *dst = smem + st * NF * PITCH;
-    if (PA) tma_load_3d(dst, &tm_a, x0 - kRadius, y0 - kRadius, plane, &bars[st]);
-    if (PB)
-      tma_load_3d(dst + (PA ? PITCH : 0), &tm_b, x0 - kRadius, y0 - kRadius,
-                  plane, &bars[st]);
+    if (M::kBoxA)
+      tma_load_3d(dst, &maps.box_a, x0 - kRadius, y0 - kRadius, plane,
+                  &bars[st]);
+    if (M::kBoxB)
+      tma_load_3d(dst + (M::kBoxA ? PITCH : 0), &maps.box_b, x0 - kRadius,
+                  y0 - kRadius, plane, &bars[st]);
   };
-  if (NF > 0 && tid == 0) {
-    const int npro = K < kStages ? K : kStages;
-    for (int k = 0; k < npro; ++k) issue(k);
+  auto issue_centre = [&](int j) {
+    const int st = j % kCStages;
+    mbar_expect_tx(&cbars[st], NC * kCBytes);
+    float *dst = cring + st * NC * CF;
+#pragma unroll
+    for (int s = 0; s < kNumCentre; ++s)
+      if (M::kMask & (1u << s))
+        tma_load_3d(dst + M::pos(s) * CF, &maps.cm[s], x0, y0, z0 + j,
+                    &cbars[st]);
+  };
+  if (tid == 0) {
+    if (NF > 0)
+      for (int k = 0; k < min(K, kStages); ++k) issue_box(k);
+    for (int j = 0; j < min(J, kCStages); ++j) issue_centre(j);
   }
 
   float4 qa[9], qb[9];
@@ -271,133 +319,167 @@ __global__ void __launch_bounds__(TileShape<TX, TY>::kThreads)
     qb[i] = qa[i];
   }
   const int brow = ly + kRadius, bcol = 4 * lx + kRadius;
+  const int coff = ly * TX + 4 * lx;  // this thread's float4 in a centre tile
 
   for (int k = 0; k < K; ++k) {
     const int st = k % kStages;
-    const int zo = z0 + (k - 2 * kRadius);  // output plane once k >= 8
-    const bool compute = k >= 2 * kRadius;
+    const int j = k - 2 * kRadius;       // output index once k >= 8
+    const int zo = z0 + j;
     const long long idx = (long long)zo * n12 + (long long)gy * n1 + gx;
-
-    // centre loads for the output plane, issued before the barrier wait
-    float4 oa = make_float4(0.f, 0.f, 0.f, 0.f), ob = oa, va = oa, vb = oa,
-           im = oa;
-    if (compute && valid) {
-      oa = ld4(p.a_old + idx);
-      if (PA || MODE == kModeSource) va = ldg4(p.a_vel + idx);
-      if (MODE != kModeSource) {
-        ob = ld4(p.b_old + idx);
-        if (PB) vb = (MODE == kModeForward) ? va : ldg4(p.b_vel + idx);
-        im = ld4(p.img + idx);
-      }
-    }
 
     bool ok = true;
     if (NF > 0) {
       ok = mbar_wait_bounded(&bars[st], (uint32_t)((k / kStages) & 1));
-      if (!ok) {
-        abort_flag = 1;
-        atomicOr(p.err, kErrWaitTimeout);
-      }
-    }
-    // newest plane's centre enters the z window
-    {
+      // newest plane's centre enters the z window
       const float *sa = smem + st * NF * PITCH;
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         qa[i] = qa[i + 1];
         qb[i] = qb[i + 1];
       }
-      if (PA) qa[8] = *reinterpret_cast<const float4 *>(sa + brow * BX + bcol);
-      if (PB)
-        qb[8] = *reinterpret_cast<const float4 *>(sa + (PA ? PITCH : 0) +
-                                                  brow * BX + bcol);
+      if (M::kBoxA)
+        qa[8] = *reinterpret_cast<const float4 *>(sa + brow * BX + bcol);
+      if (M::kBoxB)
+        qb[8] = *reinterpret_cast<const float4 *>(
+            sa + (M::kBoxA ? PITCH : 0) + brow * BX + bcol);
     }
 
-    if (compute && ok) {
+    if (j >= 0 && ok) {
+      const int cs = j % kCStages;
+      ok = mbar_wait_bounded(&cbars[cs], (uint32_t)((j / kCStages) & 1));
+      const float *cst = cring + cs * NC * CF + coff;
+      auto centre = [&](int slot) {
+        return *reinterpret_cast<const float4 *>(cst + M::pos(slot) * CF);
+      };
+      const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 oa = (M::kMask & (1u << kOldA)) ? centre(kOldA) : zero4;
+      float4 ob = (M::kMask & (1u << kOldB)) ? centre(kOldB) : zero4;
+      const float4 va = (M::kMask & (1u << kVelA)) ? centre(kVelA) : zero4;
+      const float4 vb = (M::kMask & (1u << kVelB)) ? centre(kVelB)
+                        : (MODE == kModeForward || MODE == kModeBornLin) ? va
+                                                                        : zero4;
+      const float4 im = (M::kMask & (1u << kImg)) ? centre(kImg) : zero4;
+
       const int so = (k - kRadius) % kStages;  // stage of the output plane
       const float *box_a = smem + so * NF * PITCH;
-      const float *box_b = box_a + (PA ? PITCH : 0);
+      const float *box_b = box_a + (M::kBoxA ? PITCH : 0);
       const int ez = min(zo - 4, n3 - 4 - zo);
-      const bool damp_a = (MODE != kModeSource);
-      const bool damp_b = (MODE == kModeForward);
 
       // pending source injection owed to the previous level of s (adjoint)
-      if (MODE == kModeAdjoint && PB && p.pb.active && valid)
+      if (MODE == kModeAdjoint && PB && p.pb.active && valid && ok)
         inject_row(p.pb, n1, n2, zo, gy, gx, ob);
 
-      float4 na = oa, nb = ob;
+      float4 na = oa, nb = ob, ga = zero4;
+      float bj[4];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int e = min(exy[j], ez);
+      for (int jj = 0; jj < 4; ++jj) {
+        const int e = min(exy[jj], ez);
         const float b = (e >= 0 && e < kNBound) ? s_bound[e] : 1.0f;
-        if (PA) {
+        bj[jj] = b;
+        if (M::kBoxA) {
           Nbr n;
           float c;
-          gather<BX>(box_a, brow, bcol, qa, j, n, c);
-          float old = comp(oa, j);
-          if (damp_a) old = __fmul_rn(old, b);
-          float v = leapfrog(comp(va, j), stencil_sum(p.c, c, n), c, old);
-          if (damp_a) v = __fmul_rn(v, b);
-          set_comp(na, j, v);
+          gather<BX>(box_a, brow, bcol, qa, jj, n, c);
+          float old = comp(oa, jj);
+          if (M::kDampA) old = __fmul_rn(old, b);
+          const float sa = stencil_sum(p.c, c, n);
+          set_comp(ga, jj, sa);
+          float v = leapfrog(comp(va, jj), sa, c, old);
+          // the adjoint of the linearised step injects its data before the
+          // taper (see below); every other tapered mode tapers here
+          if (MODE != kModeBornAdj && M::kDampA) v = __fmul_rn(v, b);
+          set_comp(na, jj, v);
         } else if (MODE == kModeAdjoint) {
           // receiver level not propagated (it == 0): both damping passes
-          set_comp(na, j, __fmul_rn(__fmul_rn(comp(oa, j), b), b));
+          set_comp(na, jj, __fmul_rn(__fmul_rn(comp(oa, jj), b), b));
         }
-        if (PB) {
+        if (M::kBoxB) {
           Nbr n;
           float c;
-          gather<BX>(box_b, brow, bcol, qb, j, n, c);
-          float old = comp(ob, j);
-          if (damp_b) old = __fmul_rn(old, b);
-          float v = leapfrog(comp(vb, j), stencil_sum(p.c, c, n), c, old);
-          if (damp_b) v = __fmul_rn(v, b);
-          set_comp(nb, j, v);
+          gather<BX>(box_b, brow, bcol, qb, jj, n, c);
+          float old = comp(ob, jj);
+          if (M::kDampB) old = __fmul_rn(old, b);
+          float v = leapfrog(comp(vb, jj), stencil_sum(p.c, c, n), c, old);
+          // linearised Born: scattering source m (A s) inside the taper
+          if (MODE == kModeBornLin)
+            v = __fadd_rn(v, __fmul_rn(comp(im, jj), comp(ga, jj)));
+          if (M::kDampB) v = __fmul_rn(v, b);
+          set_comp(nb, jj, v);
         }
       }
 
-      if (valid) {
-        if (p.pa.active) inject_row(p.pa, n1, n2, zo, gy, gx, na);
-        if (MODE == kModeForward) {
-          // Born coupling r += 1e-6 s img, then extraction from r
-#pragma unroll
-          for (int j = 0; j < 4; ++j)
-            set_comp(nb, j,
-                     __fadd_rn(comp(nb, j),
-                               __fmul_rn(__fmul_rn(1e-6f, comp(na, j)),
-                                         comp(im, j))));
-          if (p.pb.active) extract_row(p.pb, n1, n2, zo, gy, gx, nb);
-          st4(p.a_old + idx, na);
-          st4(p.b_old + idx, nb);
-        } else if (MODE == kModeAdjoint) {
-          // s is the new level when propagated, else the stored one
-          const float4 sv = nb;
+      if (valid && ok) {
+        if (MODE == kModeBornAdj) {
+          // w = b (v A w + 2w - b w_old + v E^T d); image += (A s) w
+          float4 inj = zero4;
+          if (p.pa.active) inject_row(p.pa, n1, n2, zo, gy, gx, inj);
           float4 ni;
-          ni.x = __fadd_rn(im.x, __fmul_rn(sv.x, na.x));
-          ni.y = __fadd_rn(im.y, __fmul_rn(sv.y, na.y));
-          ni.z = __fadd_rn(im.z, __fmul_rn(sv.z, na.z));
-          ni.w = __fadd_rn(im.w, __fmul_rn(sv.w, na.w));
-          st4(p.img + idx, ni);
-          st4(p.a_old + idx, na);
-          if (PB) st4(p.b_old + idx, nb);
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            const float w = __fmul_rn(
+                __fadd_rn(comp(na, jj), __fmul_rn(comp(va, jj), comp(inj, jj))),
+                bj[jj]);
+            set_comp(na, jj, w);
+            set_comp(ni, jj, __fadd_rn(comp(im, jj), __fmul_rn(comp(ob, jj), w)));
+          }
+          st4(p.img_out + idx, ni);
+          st4(p.a_out + idx, na);
         } else {
-          st4(p.a_old + idx, na);
+          if (p.pa.active) inject_row(p.pa, n1, n2, zo, gy, gx, na);
+          if (MODE == kModeForward) {
+            // Born coupling r += 1e-6 s img, then extraction from r
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj)
+              set_comp(nb, jj,
+                       __fadd_rn(comp(nb, jj),
+                                 __fmul_rn(__fmul_rn(1e-6f, comp(na, jj)),
+                                           comp(im, jj))));
+          }
+          if (MODE == kModeForward || MODE == kModeBornLin) {
+            if (p.pb.active) extract_row(p.pb, n1, n2, zo, gy, gx, nb);
+            st4(p.a_out + idx, na);
+            st4(p.b_out + idx, nb);
+          } else if (MODE == kModeAdjoint) {
+            // s is the new level when propagated, else the stored one
+            float4 ni;
+            ni.x = __fadd_rn(im.x, __fmul_rn(nb.x, na.x));
+            ni.y = __fadd_rn(im.y, __fmul_rn(nb.y, na.y));
+            ni.z = __fadd_rn(im.z, __fmul_rn(nb.z, na.z));
+            ni.w = __fadd_rn(im.w, __fmul_rn(nb.w, na.w));
+            st4(p.img_out + idx, ni);
+            st4(p.a_out + idx, na);
+            if (PB) st4(p.b_out + idx, nb);
+          } else {  // source, model
+            if (MODE == kModeModel) {
+              if (p.pb.active) extract_row(p.pb, n1, n2, zo, gy, gx, na);
+              if (p.g_out) st4(p.g_out + idx, ga);
+            }
+            st4(p.a_out + idx, na);
+          }
         }
       }
+    }
+    if (!ok) {
+      abort_flag = 1;
+      atomicOr(p.err, kErrWaitTimeout);
     }
 
     __syncthreads();
     if (abort_flag) break;
-    if (NF > 0 && tid == 0 && k >= kRadius && k - kRadius + kStages < K) {
+    if (tid == 0) {
       fence_proxy_async();
-      issue(k - kRadius + kStages);
+      if (NF > 0 && k >= kRadius && k - kRadius + kStages < K)
+        issue_box(k - kRadius + kStages);
+      if (j >= 0 && j + kCStages < J) issue_centre(j + kCStages);
     }
   }
 
-  if (NF > 0 && abort_flag && tid == 0) {
+  if (abort_flag && tid == 0) {
     // drain whatever is still in flight (bounded) before the CTA retires
-    for (int s = 0; s < kStages; ++s) {
-      uint64_t t0 = global_ns();
-      while (!mbar_try_wait(&bars[s], 0) && !mbar_try_wait(&bars[s], 1) &&
+    for (int s = 0; s < kStages + kCStages; ++s) {
+      uint64_t *b = s < kStages ? &bars[s] : &cbars[s - kStages];
+      const uint64_t t0 = global_ns();
+      while (!mbar_try_wait(b, 0) && !mbar_try_wait(b, 1) &&
              global_ns() - t0 < 100000000ull) {
       }
     }
@@ -412,19 +494,34 @@ __global__ void point_inject_kernel(const PointSet ps, int npts,
         __fadd_rn(field[ps.slot_cell[s]], point_value(ps, ps.slot_index[s]));
 }
 
+__global__ void divide_kernel(const float *a, const float *v, float *out,
+                              long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = v[i] != 0.f ? __fdiv_rn(a[i], v[i]) : 0.f;
+}
+
 // ---------------------------------------------------------------------------
 struct TileCfg {
   int tx, ty;
 };
-constexpr TileCfg kTileCfgs[] = {{64, 16}, {32, 16}, {32, 32}, {64, 8}};
+constexpr TileCfg kTileCfgs[] = {{64, 16}, {32, 16}, {32, 32}, {64, 8},
+                                 {32, 8}};
 constexpr int kNumTileCfgs = sizeof(kTileCfgs) / sizeof(kTileCfgs[0]);
 
 template <int MODE, bool PA, bool PB, int TX, int TY>
-cudaError_t launch_t(const CUtensorMap &tm_a, const CUtensorMap &tm_b,
-                     const StepParams &p, cudaStream_t stream) {
-  using T = TileShape<TX, TY>;
-  constexpr int NF = (PA ? 1 : 0) + (PB ? 1 : 0);
-  const size_t smem = (size_t)kStages * NF * T::kBoxPitch * 4 + 128;
+size_t smem_bytes_t() {
+  using M = ModeTraits<MODE, PA, PB>;
+  using T = Tile<TX, TY>;
+  return (size_t)kStages * M::kNF * T::kBoxPitch * 4 +
+         (size_t)kCStages * M::kNC * T::kCFloats * 4 + 128;
+}
+
+template <int MODE, bool PA, bool PB, int TX, int TY>
+cudaError_t launch_t(const StepMaps &maps, const StepParams &p,
+                     cudaStream_t stream) {
+  using T = Tile<TX, TY>;
+  const size_t smem = smem_bytes_t<MODE, PA, PB, TX, TY>();
   auto kern = step_kernel<MODE, PA, PB, TX, TY>;
   static bool configured = false;
   if (!configured) {
@@ -435,32 +532,70 @@ cudaError_t launch_t(const CUtensorMap &tm_a, const CUtensorMap &tm_b,
   }
   const int nseg = (p.n3 - 2 * kRadius + p.zseg - 1) / p.zseg;
   dim3 grid(p.tiles_x * p.tiles_y, nseg);
-  kern<<<grid, T::kThreads, smem, stream>>>(tm_a, tm_b, p);
+  kern<<<grid, T::kThreads, smem, stream>>>(maps, p);
   return cudaGetLastError();
 }
 
-template <int TX, int TY>
-cudaError_t launch_cfg(int mode, bool pa, bool pb, const CUtensorMap &tm_a,
-                       const CUtensorMap &tm_b, const StepParams &p,
-                       cudaStream_t s) {
+// Dispatch over (mode, pa, pb) for one tile shape; F::go is instantiated
+// for every variant.
+template <int TX, int TY, class F>
+auto dispatch(int mode, bool pa, bool pb, F f) {
   switch (mode) {
-    case kModeSource:
-      return launch_t<kModeSource, true, false, TX, TY>(tm_a, tm_b, p, s);
-    case kModeForward:
-      return launch_t<kModeForward, true, true, TX, TY>(tm_a, tm_b, p, s);
-    case kModeAdjoint:
-      if (pa && pb)
-        return launch_t<kModeAdjoint, true, true, TX, TY>(tm_a, tm_b, p, s);
-      if (pa)
-        return launch_t<kModeAdjoint, true, false, TX, TY>(tm_a, tm_b, p, s);
-      if (pb)
-        return launch_t<kModeAdjoint, false, true, TX, TY>(tm_a, tm_b, p, s);
-      return launch_t<kModeAdjoint, false, false, TX, TY>(tm_a, tm_b, p, s);
+    case kModeSource: return f.template go<kModeSource, true, false, TX, TY>();
+    case kModeForward: return f.template go<kModeForward, true, true, TX, TY>();
+    case kModeModel: return f.template go<kModeModel, true, false, TX, TY>();
+    case kModeBornLin: return f.template go<kModeBornLin, true, true, TX, TY>();
+    case kModeBornAdj: return f.template go<kModeBornAdj, true, false, TX, TY>();
+    default:
+      if (pa && pb) return f.template go<kModeAdjoint, true, true, TX, TY>();
+      if (pa) return f.template go<kModeAdjoint, true, false, TX, TY>();
+      if (pb) return f.template go<kModeAdjoint, false, true, TX, TY>();
+      return f.template go<kModeAdjoint, false, false, TX, TY>();
   }
-  return cudaErrorInvalidValue;
+}
+
+struct LaunchF {
+  const StepMaps &maps;
+  const StepParams &p;
+  cudaStream_t s;
+  template <int MODE, bool PA, bool PB, int TX, int TY>
+  cudaError_t go() const {
+    return launch_t<MODE, PA, PB, TX, TY>(maps, p, s);
+  }
+};
+
+struct SmemF {
+  template <int MODE, bool PA, bool PB, int TX, int TY>
+  size_t go() const {
+    return smem_bytes_t<MODE, PA, PB, TX, TY>();
+  }
+};
+
+template <class F>
+auto dispatch_cfg(int cfg, int mode, bool pa, bool pb, F f) {
+  switch (cfg) {
+    case 1: return dispatch<32, 16>(mode, pa, pb, f);
+    case 2: return dispatch<32, 32>(mode, pa, pb, f);
+    case 3: return dispatch<64, 8>(mode, pa, pb, f);
+    case 4: return dispatch<32, 8>(mode, pa, pb, f);
+    default: return dispatch<64, 16>(mode, pa, pb, f);
+  }
 }
 
 }  // namespace
+
+unsigned centre_mask(int mode, bool pa, bool pb) {
+  switch (mode) {
+    case kModeSource: return ModeTraits<kModeSource, true, false>::kMask;
+    case kModeForward: return ModeTraits<kModeForward, true, true>::kMask;
+    case kModeModel: return ModeTraits<kModeModel, true, false>::kMask;
+    case kModeBornLin: return ModeTraits<kModeBornLin, true, true>::kMask;
+    case kModeBornAdj: return ModeTraits<kModeBornAdj, true, false>::kMask;
+    default:
+      return (1u << kOldA) | (1u << kOldB) | (1u << kImg) |
+             (pa ? (1u << kVelA) : 0u) | (pb ? (1u << kVelB) : 0u);
+  }
+}
 
 int tile_cfg_count() { return kNumTileCfgs; }
 
@@ -469,29 +604,28 @@ void tile_cfg_dims(int cfg, int *tx, int *ty) {
   *ty = kTileCfgs[cfg].ty;
 }
 
-size_t step_smem_bytes(int cfg, int nfields) {
-  const int bx = kTileCfgs[cfg].tx + 8, by = kTileCfgs[cfg].ty + 8;
-  const size_t pitch = ((size_t)bx * by * 4 + 127) / 128 * 128;
-  return (size_t)kStages * nfields * pitch + 128;
+size_t step_smem_bytes(int cfg, int mode, bool pa, bool pb) {
+  return dispatch_cfg(cfg, mode, pa, pb, SmemF{});
 }
 
 cudaError_t launch_step(int mode, bool pa, bool pb, int cfg,
-                        const CUtensorMap &tm_a, const CUtensorMap &tm_b,
-                        const StepParams &p, cudaStream_t s) {
-  if (mode == kModeSource && (!pa || pb)) return cudaErrorInvalidValue;
-  if (mode == kModeForward && !(pa && pb)) return cudaErrorInvalidValue;
-  switch (cfg) {
-    case 0: return launch_cfg<64, 16>(mode, pa, pb, tm_a, tm_b, p, s);
-    case 1: return launch_cfg<32, 16>(mode, pa, pb, tm_a, tm_b, p, s);
-    case 2: return launch_cfg<32, 32>(mode, pa, pb, tm_a, tm_b, p, s);
-    case 3: return launch_cfg<64, 8>(mode, pa, pb, tm_a, tm_b, p, s);
-  }
-  return cudaErrorInvalidValue;
+                        const StepMaps &maps, const StepParams &p,
+                        cudaStream_t s) {
+  if (mode < kModeSource || mode > kModeBornAdj) return cudaErrorInvalidValue;
+  if (cfg < 0 || cfg >= kNumTileCfgs) return cudaErrorInvalidValue;
+  return dispatch_cfg(cfg, mode, pa, pb, LaunchF{maps, p, s});
 }
 
 cudaError_t launch_point_inject(const PointSet &ps, int npts, float *field,
                                 cudaStream_t stream) {
   point_inject_kernel<<<1, 32, 0, stream>>>(ps, npts, field);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_divide(const float *a, const float *v, float *out,
+                          long long n, cudaStream_t stream) {
+  const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+  divide_kernel<<<blocks, 256, 0, stream>>>(a, v, out, n);
   return cudaGetLastError();
 }
 

@@ -3,14 +3,18 @@
 // One launch advances one FD time step of one or two coupled wavefields over
 // the interior [4, n-4)^3 of a [n3][n2][n1] float grid (n1 fastest).  Work is
 // split into xy tiles (TX x TY cells) and z segments; each CTA marches its
-// segment plane by plane.  The current wavefield of every propagated field is
-// brought in by TMA (cp.async.bulk.tensor.3d) as a (TX+8) x (TY+8) box per
-// plane into an S-stage shared-memory ring guarded by mbarriers; the x/y
-// neighbours come from that box, the 9-plane z window lives in registers.
-// The previous level, velocity and image are read once per cell with float4
-// loads and the new level is written once, so HBM sees the compulsory bytes.
+// segment plane by plane.  All HBM reads are asynchronous TMA copies
+// (cp.async.bulk.tensor.3d) completing on mbarriers:
+//   * box ring: the current level of every propagated field, one
+//     (TX+8) x (TY+8) box per plane, kStages deep; x/y neighbours come from
+//     the box, the 9-plane z window is kept in registers;
+//   * centre ring: the per-cell inputs of the output plane (previous levels,
+//     velocities, image or reflectivity), one TX x TY tile each, kCStages
+//     deep.
+// The new level (and the image) are written once with float4 stores, so HBM
+// sees the compulsory bytes only.
 //
-// What is fused into the pass (reference base/cpu_prop.cc):
+// Reference semantics fused into the pass (base/cpu_prop.cc):
 //   prop (224-253)       stencil, same left-to-right sum, no FMA contraction
 //   damp (141-165)       the new level is scaled by b(edge); the scaling that
 //                        the reference applies in place to the current level
@@ -20,6 +24,9 @@
 //   imageAdd (216-223)   Born coupling r += 1e-6 s img
 //   dataExtract (198-215) receiver traces accumulate in place
 //   imageCondition (97-105) img += s r
+// plus the exact linearised Born pair (modes kModeBornLin / kModeBornAdj)
+// and plain nonlinear modelling (kModeModel), used for the dot-product and
+// finite-difference checks and for least-squares migration.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -30,7 +37,14 @@ namespace born {
 constexpr int kRadius = 4;
 constexpr int kNBound = 40;  // taper table length (cpu_prop.cc:329-332)
 
-enum StepMode : int { kModeSource = 0, kModeForward = 1, kModeAdjoint = 2 };
+enum StepMode : int {
+  kModeSource = 0,   // sourceProp step (one field, no taper)
+  kModeForward = 1,  // rtmForward step (s and r, taper, 1e-6 coupling)
+  kModeAdjoint = 2,  // rtmAdjoint step (r with taper, s rebuilt, image)
+  kModeModel = 3,    // nonlinear modelling step with taper (+ A s output)
+  kModeBornLin = 4,  // exact linearised Born step: r += m * (A s) inside taper
+  kModeBornAdj = 5,  // its exact adjoint: w step, image += g * w
+};
 
 // Device view of a set of points (sources or receivers) on the grid.
 // Points are sorted by cell, then by their original index; plane_off[z] is
@@ -50,56 +64,55 @@ struct PointSet {
   float tab[8];           // sinc row for this step
 };
 
+// Centre-tile slots (TMA maps cm[slot] in the launch)
+enum CentreSlot : int { kOldA = 0, kOldB = 1, kVelA = 2, kVelB = 3, kImg = 4 };
+constexpr int kNumCentre = 5;
+
 struct StepParams {
   int n1, n2, n3;
   int tiles_x, tiles_y, zseg;
   float c[13];             // stencil coefficients, slots as cpu_prop.cc:6-18
   float bound[kNBound];
-  // field A: source mode p, forward s, adjoint r
-  const float *a_cur;
-  float *a_old;            // previous level in, new level out
-  const float *a_vel;
-  // field B: forward r, adjoint s
-  const float *b_cur;
-  float *b_old;
-  const float *b_vel;
-  float *img;              // forward: reflectivity (read); adjoint: image
+  // outputs (in-place over the previous level)
+  float *a_out;            // field A: source p / forward s / adjoint r / w
+  float *b_out;            // field B: forward r / adjoint s
+  float *img_out;          // adjoint image (read through the centre ring)
+  float *g_out;            // kModeModel: A s of the current level, or null
   PointSet pa;             // injection into the new level of A
-  PointSet pb;             // forward: extraction from B; adjoint: injection
-                           // still owed to B's previous level
+  PointSet pb;             // forward / linearised: extraction from B;
+                           // adjoint: injection owed to B's previous level;
+                           // model: extraction from A
   unsigned int *err;       // device error word (bit 0: mbarrier wait gave up)
 };
 
 constexpr unsigned int kErrWaitTimeout = 1u;
+constexpr int kStages = 8;   // box ring depth (planes)
+constexpr int kCStages = 4;  // centre ring depth (output planes)
 
-template <int TX, int TY>
-struct TileShape {
-  static constexpr int kTX = TX, kTY = TY;
-  static constexpr int kBX = TX + 2 * kRadius, kBY = TY + 2 * kRadius;
-  static constexpr int kBoxFloats = kBX * kBY;
-  // stage pitch rounded to 128 B (TMA destination alignment)
-  static constexpr int kBoxPitch = ((kBoxFloats * 4 + 127) / 128) * 32;
-  static constexpr int kThreads = (TX / 4) * TY;
+struct StepMaps {
+  CUtensorMap box_a, box_b;       // halo boxes of the current levels
+  CUtensorMap cm[kNumCentre];     // centre tiles, by CentreSlot
 };
 
-constexpr int kStages = 8;
-
-// Host-side launch entry (defined in born_step.cu).  tm_a / tm_b are the
-// tensor maps of the current level of field A / B (unused ones may be any
-// valid map).  pa/pb flags say which fields are propagated this step.
+// Host-side launch entry (defined in born_step.cu).  prop_a / prop_b say
+// which fields are propagated this step (adjoint first/last steps).
 cudaError_t launch_step(int mode, bool prop_a, bool prop_b, int tile_cfg,
-                        const CUtensorMap &tm_a, const CUtensorMap &tm_b,
-                        const StepParams &p, cudaStream_t stream);
+                        const StepMaps &maps, const StepParams &p,
+                        cudaStream_t stream);
+
+// Which centre slots a mode reads (bit mask over CentreSlot).
+unsigned centre_mask(int mode, bool prop_a, bool prop_b);
 
 // Tile configurations (index -> TX, TY).
 int tile_cfg_count();
 void tile_cfg_dims(int cfg, int *tx, int *ty);
-size_t step_smem_bytes(int tile_cfg, int nfields);
+size_t step_smem_bytes(int tile_cfg, int mode, bool prop_a, bool prop_b);
 
-// Small kernel: add a pending injection into a buffer at the points of a set
-// (used once at the end of the adjoint so the source level left in memory
-// matches the reference's in-place injection).
+// Small kernels.
 cudaError_t launch_point_inject(const PointSet &ps, int npts, float *field,
                                 cudaStream_t stream);
+// out[i] = a[i] / v[i] over the whole grid (image of the exact adjoint).
+cudaError_t launch_divide(const float *a, const float *v, float *out,
+                          long long n, cudaStream_t stream);
 
 }  // namespace born
