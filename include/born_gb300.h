@@ -169,10 +169,73 @@ int born_set_source_levels(born_handle *h, const float *p0, const float *p1);
 int born_zero_traces(born_handle *h);
 int born_synchronize(born_handle *h);
 
+/* ======================================================================
+ * 3. Born operator (model image <-> shot data) and CG least squares
+ *
+ * born_op is rtm_zero_op (base/rtm_zero_op_3d.h:10-43) behind the
+ * my_operator contract forward/adjoint(add, model, data)
+ * (base/my_operator.h:18-25): add = 0 zeroes the output first.  Unlike the
+ * reference (which reads the model from a file member and writes data to a
+ * file, rtm_zero_op_3d.cc:161,193,295) it reads and writes the vectors it is
+ * given.  Vectors are DEVICE pointers on the handle's device:
+ *   model: velocity/image grid n3 x n2 x n1 floats,
+ *   data:  nshots x rec_ny x rec_nx x nt_data floats (time fastest).
+ * exact = 0 reproduces rtm_zero_op (random-boundary RTM adjoint, 1e-6 Born
+ * coupling); exact = 1 uses the exact linearised pair, so adjoint is the
+ * transpose of forward (dot-product test) and CG converges.
+ * ====================================================================== */
+typedef struct born_op born_op;
+typedef struct {
+  int n1, n2, n3;          /* model grid (velocity and image) */
+  float o1, o2, o3, d1, d2, d3;
+  int nt_data;             /* data time samples */
+  float dt_data;
+  int rec_nx, rec_ny;      /* receiver grid at rec_depth */
+  float rec_ox, rec_dx, rec_oy, rec_dy, rec_depth;
+  int nshots;              /* shot positions given to born_op_create */
+  int nt_wavelet;          /* raw source wavelet (its time derivative is
+                              injected, source_func_3d.cc:120-124) */
+  float dt_wavelet;
+  int nbound;              /* absorbing / random boundary cells (fd_prop_3d.cc:48-53) */
+  int exact;               /* 0: reference operator, 1: exact linearised pair */
+  int ckpt_interval;       /* exact adjoint checkpoint interval (0: 50) */
+} born_op_params;
+
+/* velocity: host n3 x n2 x n1 m/s; shots: host nshots x (x, y, z);
+ * wavelet: host nt_wavelet samples.  Builds the compute grid, sinc tables,
+ * receiver and source geometry and the v^2 dt^2 models (one random-boundary
+ * model per shot in reference mode) on the device of h. */
+int born_op_create(born_handle *h, const born_op_params *p,
+                   const float *velocity, const float *shots,
+                   const float *wavelet, born_op **out);
+int born_op_destroy(born_op *op);
+int born_op_sizes(const born_op *op, long long *model_n, long long *data_n,
+                  int *nt_fd, float *dt_fd);
+int born_op_forward(born_op *op, int add, const float *model, float *data);
+int born_op_adjoint(born_op *op, int add, float *model, const float *data);
+/* FP64 dot product of two device float vectors (block partials in double). */
+int born_dot_f64(born_op *op, const float *a, const float *b, long long n,
+                 double *out);
+/* Least squares by Claerbout's CG (lin_solver.cc:104-132, cgstep.cc:11-54):
+ * model (device, in: starting model, out: solution); resid (host, niter+1
+ * doubles, nullable) receives rr.rr before and after every iteration. */
+int born_cg_solve(born_op *op, const float *data, float *model, int niter,
+                  double *resid);
+
 /* Tuning: tile configuration index (0..born_tile_config_count()-1, or -1 for
  * the built-in choice) and z-segment depth (0 = automatic). */
 int born_tile_config_count(void);
 int born_set_tiling(born_handle *h, int tile_cfg, int zseg);
+/* Autotuner: with enable != 0, times every tile configuration of each step
+ * mode on the current grid now (needs the grid and both velocities) and
+ * uses the fastest; time loops also tune a mode lazily on first use while
+ * enabled and no fixed tiling is set.  enable = 0 turns it off. */
+int born_autotune(born_handle *h, int enable);
+/* Tile configuration in use for a step mode (0 source, 1 rtm forward,
+ * 2 rtm adjoint, 3 modelling, 4 linearised forward, 5 its adjoint) and the
+ * tuner's time per launch. */
+int born_tuned_config(const born_handle *h, int mode, int *cfg,
+                      float *ms_per_launch);
 /* Kernels launched on this handle since creation (for accounting). */
 long long born_kernel_launches(const born_handle *h);
 /* Raw CUDA stream of the handle (cudaStream_t), for event timing. */

@@ -81,8 +81,21 @@ _SIGS = {
     "born_synchronize": (C.c_int, [_vp]),
     "born_tile_config_count": (C.c_int, []),
     "born_set_tiling": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "born_autotune": (C.c_int, [_vp, C.c_int]),
+    "born_tuned_config": (C.c_int, [_vp, C.c_int, _ip, _fp]),
     "born_kernel_launches": (C.c_longlong, [_vp]),
     "born_stream": (_vp, [_vp]),
+    # operator and CG (include/born_gb300.h section 3)
+    "born_op_create": (C.c_int, [_vp, _vp, _fp, _fp, _fp, C.POINTER(_vp)]),
+    "born_op_destroy": (C.c_int, [_vp]),
+    "born_op_sizes": (C.c_int, [_vp, C.POINTER(C.c_longlong),
+                                C.POINTER(C.c_longlong), _ip, _fp]),
+    "born_op_forward": (C.c_int, [_vp, C.c_int, _vp, _vp]),
+    "born_op_adjoint": (C.c_int, [_vp, C.c_int, _vp, _vp]),
+    "born_dot_f64": (C.c_int, [_vp, _vp, _vp, C.c_longlong,
+                               C.POINTER(C.c_double)]),
+    "born_cg_solve": (C.c_int, [_vp, _vp, _vp, C.c_int,
+                                C.POINTER(C.c_double)]),
     # host geometry (csrc/born_host.h)
     "born_sinc_table": (C.c_int, [C.c_int, C.c_int, _fp]),
     "born_calc_stability": (C.c_float, [C.c_float, C.c_float, C.c_float,
@@ -203,6 +216,15 @@ class Handle:
 
     def set_tiling(self, cfg: int = -1, zseg: int = 0):
         self.check(self.lib.born_set_tiling(self.h, cfg, zseg))
+
+    def autotune(self, enable: bool = True):
+        self.check(self.lib.born_autotune(self.h, int(enable)))
+
+    def tuned_config(self, mode: int):
+        cfg, ms = C.c_int(), C.c_float()
+        self.check(self.lib.born_tuned_config(self.h, mode, C.byref(cfg),
+                                              C.byref(ms)))
+        return cfg.value, ms.value
 
     def synchronize(self):
         self.check(self.lib.born_synchronize(self.h))
@@ -345,6 +367,98 @@ class Gb300Prop(Handle):
 
     def zero_traces(self):
         self.check(self.lib.born_zero_traces(self.h))
+
+
+# ---------------------------------------------------------------------------
+# Born operator (rtm_zero_op behind the my_operator contract) and CG
+
+class OpParams(C.Structure):
+    _fields_ = [("n1", C.c_int), ("n2", C.c_int), ("n3", C.c_int),
+                ("o1", C.c_float), ("o2", C.c_float), ("o3", C.c_float),
+                ("d1", C.c_float), ("d2", C.c_float), ("d3", C.c_float),
+                ("nt_data", C.c_int), ("dt_data", C.c_float),
+                ("rec_nx", C.c_int), ("rec_ny", C.c_int),
+                ("rec_ox", C.c_float), ("rec_dx", C.c_float),
+                ("rec_oy", C.c_float), ("rec_dy", C.c_float),
+                ("rec_depth", C.c_float), ("nshots", C.c_int),
+                ("nt_wavelet", C.c_int), ("dt_wavelet", C.c_float),
+                ("nbound", C.c_int), ("exact", C.c_int),
+                ("ckpt_interval", C.c_int)]
+
+
+class BornOperator(Handle):
+    """rtm_zero_op (base/rtm_zero_op_3d.cc) with the my_operator contract
+    forward/adjoint(add, model, data) (base/my_operator.h:18-25).
+
+    model / data are CUDA tensors (float32, contiguous) on this handle's
+    device: model [n3, n2, n1], data [nshots, rec_ny, rec_nx, nt_data].
+    ``exact=True`` selects the exact linearised pair (adjoint = transpose).
+    """
+
+    def __init__(self, velocity, o, d, shots, wavelet, dt_wavelet, nt_data,
+                 dt_data, rec_n, rec_o, rec_d, rec_depth, nbound,
+                 exact=False, ckpt_interval=50, device=0):
+        super().__init__(device)
+        vel = f32(velocity)
+        n3, n2, n1 = vel.shape
+        shots = f32(shots).reshape(-1, 3)
+        wav = f32(wavelet)
+        self.params = OpParams(n1, n2, n3, o[0], o[1], o[2], d[0], d[1], d[2],
+                               nt_data, dt_data, rec_n[0], rec_n[1],
+                               rec_o[0], rec_d[0], rec_o[1], rec_d[1],
+                               rec_depth, shots.shape[0], wav.size,
+                               dt_wavelet, nbound, int(exact), ckpt_interval)
+        op = _vp()
+        self.check(self.lib.born_op_create(self.h, C.byref(self.params),
+                                           fptr(vel), fptr(shots), fptr(wav),
+                                           C.byref(op)))
+        self.op = op
+        mn, dn = C.c_longlong(), C.c_longlong()
+        nt, dt = C.c_int(), C.c_float()
+        self.check(self.lib.born_op_sizes(op, C.byref(mn), C.byref(dn),
+                                          C.byref(nt), C.byref(dt)))
+        self.model_shape = (n3, n2, n1)
+        self.data_shape = (shots.shape[0], rec_n[1], rec_n[0], nt_data)
+        self.nt_fd, self.dt_fd = nt.value, dt.value
+
+    def close(self):
+        if getattr(self, "op", None):
+            self.lib.born_op_destroy(self.op)
+            self.op = None
+        super().close()
+
+    @staticmethod
+    def _dev(t, shape):
+        assert t.is_cuda and t.dtype.itemsize == 4 and t.is_contiguous()
+        assert tuple(t.shape) == tuple(shape), (t.shape, shape)
+        return C.c_void_p(t.data_ptr())
+
+    def forward(self, add, model, data):
+        self.check(self.lib.born_op_forward(
+            self.op, int(add), self._dev(model, self.model_shape),
+            self._dev(data, self.data_shape)))
+        return True
+
+    def adjoint(self, add, model, data):
+        self.check(self.lib.born_op_adjoint(
+            self.op, int(add), self._dev(model, self.model_shape),
+            self._dev(data, self.data_shape)))
+        return True
+
+    def dot(self, a, b):
+        out = C.c_double()
+        self.check(self.lib.born_dot_f64(self.op, C.c_void_p(a.data_ptr()),
+                                         C.c_void_p(b.data_ptr()), a.numel(),
+                                         C.byref(out)))
+        return out.value
+
+    def cg(self, data, model, niter):
+        """Least squares by cgstep CG; model is updated in place."""
+        res = (C.c_double * (niter + 1))()
+        self.check(self.lib.born_cg_solve(
+            self.op, self._dev(data, self.data_shape),
+            self._dev(model, self.model_shape), niter, res))
+        return list(res)
 
 
 # ---------------------------------------------------------------------------

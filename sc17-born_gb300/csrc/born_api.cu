@@ -20,8 +20,7 @@
 #include <utility>
 #include <vector>
 
-#include "../../include/born_gb300.h"
-#include "born_step.cuh"
+#include "born_internal.h"
 
 using born::kModeAdjoint;
 using born::kModeForward;
@@ -52,60 +51,7 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// Device copy of one point set (sources or receivers).
-struct DevPoints {
-  int npts = 0, nt = 0;
-  int *plane_off = nullptr, *cell_head = nullptr, *slot_cell = nullptr,
-      *slot_index = nullptr;
-  float *traces = nullptr;
-  size_t traces_cap = 0;
-  void release() {
-    cudaFree(plane_off);
-    cudaFree(cell_head);
-    cudaFree(slot_cell);
-    cudaFree(slot_index);
-    cudaFree(traces);
-    *this = DevPoints();
-  }
-};
-
 }  // namespace
-
-struct born_handle {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  std::string err;
-  // grid
-  bool have_space = false;
-  int n1 = 0, n2 = 0, n3 = 0;
-  long long n123 = 0;
-  float coeffs[13] = {};
-  float bound[born::kNBound] = {};
-  // sinc tables (rows x 8)
-  int jt_s = 0, jt_d = 0;
-  std::vector<float> tab_s, tab_d;
-  int jt = 1;  // the reference's _jt: last jt given to a time loop
-  // device fields
-  float *vel1 = nullptr, *vel2 = nullptr;
-  float *s0 = nullptr, *s1 = nullptr;  // source levels (p0, p1 of source_prop)
-  float *r0 = nullptr, *r1 = nullptr;  // receiver / scattered levels
-  float *f0 = nullptr, *f1 = nullptr;  // forward background levels
-  float *img = nullptr, *refl = nullptr;
-  unsigned int *err_dev = nullptr;
-  bool have_vel1 = false, have_vel2 = false, have_refl = false;
-  DevPoints src, rec;
-  bool src_levels_valid = false;
-  const float *host_p0 = nullptr, *host_p1 = nullptr;
-  int tile_cfg = -1, zseg = 0;
-  long long launches = 0;
-  int ntblock = 0;
-  // TMA descriptors by (buffer, tile config * 2 + kind); kind 0 = halo box,
-  // 1 = centre tile
-  std::map<std::pair<const void *, int>, CUtensorMap> maps;
-  // exact linearised adjoint: checkpoints and the per-segment A s buffer
-  float *ckpt = nullptr, *gbuf = nullptr;
-  size_t ckpt_levels = 0, gbuf_levels = 0;
-};
 
 namespace {
 
@@ -216,6 +162,10 @@ int upload_points(born_handle *h, DevPoints &dp, int npts, int nt,
   DevPoints nd;
   nd.npts = npts;
   nd.nt = nt;
+  for (int z : planes) {
+    nd.zlo = std::min(nd.zlo, z);
+    nd.zhi = std::max(nd.zhi, z);
+  }
   CK(h, cudaMalloc(&nd.plane_off, sizeof(int) * h->n3));
   CK(h, cudaMalloc(&nd.cell_head, sizeof(int) * head.size()));
   CK(h, cudaMalloc(&nd.slot_cell, sizeof(int) * std::max(1, npts)));
@@ -270,11 +220,13 @@ int get_map(born_handle *h, const float *buf, int cfg, int kind,
   return BORN_OK;
 }
 
-// Tiling: the configured one, else 32x16 tiles; z segments sized so that
-// the grid covers every SM a few times.
+// Tiling: the configured one, else the autotuned one for the mode, else
+// 64x16 tiles; z segments sized so that the grid covers every SM a few times.
 void pick_tiling(born_handle *h, int mode, bool pa, bool pb, int *cfg,
                  int *zseg, int *tiles_x, int *tiles_y) {
-  int c = h->tile_cfg >= 0 ? h->tile_cfg : 1;
+  int c = h->tile_cfg >= 0                ? h->tile_cfg
+          : h->tuned_cfg[mode] >= 0 ? h->tuned_cfg[mode]
+                                          : 0;
   int tx, ty;
   born::tile_cfg_dims(c, &tx, &ty);
   *cfg = c;
@@ -308,6 +260,8 @@ PointSet point_view(const DevPoints &dp, int id, int ii,
   ps.traces = dp.traces;
   ps.npts = dp.npts;
   ps.nt_trace = dp.nt;
+  ps.zlo = dp.zlo;
+  ps.zhi = dp.zhi;
   ps.id = id;
   ps.scale = scale;
   ps.active = use && dp.npts > 0 && (id + 7 < dp.nt) ? 1 : 0;
@@ -353,6 +307,64 @@ int launch(born_handle *h, int mode, bool pa, bool pb, const float *a_cur,
   return BORN_OK;
 }
 
+int check_device_error(born_handle *h);
+
+// Autotuner: times every tile configuration of one step mode on the
+// current grid (one warm-up and three timed launches, CUDA events on the
+// handle's stream) and keeps the fastest.  It runs on the scratch levels
+// f0/f1/r0/r1 and the image with every point set inactive, so it never
+// touches the source levels kept for rtm_adjoint, and clears what it used.
+int tune_mode(born_handle *h, int mode) {
+  const bool pb = mode == kModeForward || mode == kModeAdjoint ||
+                  mode == born::kModeBornLin;
+  if (!h->have_vel1 || !h->have_vel2) return BORN_OK;  // nothing to time yet
+  cudaEvent_t e0, e1;
+  CK(h, cudaEventCreate(&e0));
+  CK(h, cudaEventCreate(&e1));
+  const int saved = h->tile_cfg;
+  int best = -1;
+  float best_ms = 0.f;
+  int rc = BORN_OK;
+  for (int cfg = 0; cfg < born::tile_cfg_count() && !rc; ++cfg) {
+    h->tile_cfg = cfg;
+    StepParams p;
+    base_params(h, p);
+    p.a_out = h->f1;
+    p.b_out = h->r1;
+    p.img_out = h->img;
+    const float *cen[born::kNumCentre] = {h->f1, h->r1, h->vel2, h->vel1,
+                                          h->img};
+    for (int it = 0; it < 4 && !rc; ++it) {
+      if (it == 1) cudaEventRecord(e0, h->stream);
+      rc = launch(h, mode, true, pb, h->f0, h->r0, cen, p);
+    }
+    cudaEventRecord(e1, h->stream);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (!rc && (best < 0 || ms < best_ms)) {
+      best = cfg;
+      best_ms = ms;
+    }
+  }
+  h->tile_cfg = saved;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  h->tuned_cfg[mode] = best;
+  h->tuned_ms[mode] = best_ms / 3.f;
+  const size_t bytes = (size_t)h->n123 * 4;
+  float *scratch[] = {h->f0, h->f1, h->r0, h->r1, h->img};
+  for (float *b : scratch) CK(h, cudaMemsetAsync(b, 0, bytes, h->stream));
+  return check_device_error(h);
+}
+
+int ensure_tuned(born_handle *h, int mode) {
+  if (!h->autotune || h->tile_cfg >= 0 || h->tuned_cfg[mode] >= 0)
+    return BORN_OK;
+  return tune_mode(h, mode);
+}
+
 // Every this many steps the loops look at the device error word, so that a
 // kernel whose bounded wait gave up stops the loop instead of being followed
 // by thousands of launches that would each exit early.
@@ -391,6 +403,18 @@ int check_device_error(born_handle *h) {
 }
 
 }  // namespace
+
+int born_fail(born_handle *h, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf;
+  return code;
+}
+int born_check_ready(born_handle *h) { return check_ready(h); }
+int born_check_device_error(born_handle *h) { return check_device_error(h); }
 
 // ===========================================================================
 // Handle API
@@ -543,6 +567,8 @@ int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
   if (!h->have_vel1) return fail(h, BORN_ESTATE, "vel1 not transferred");
   if (h->jt_s < 1) return fail(h, BORN_ESTATE, "source sinc table missing");
   h->jt = jts;
+  rc = ensure_tuned(h, kModeSource);
+  if (rc) return rc;
   const size_t bytes = (size_t)h->n123 * 4;
   CK(h, cudaMemsetAsync(h->s0, 0, bytes, h->stream));
   CK(h, cudaMemsetAsync(h->s1, 0, bytes, h->stream));
@@ -584,6 +610,8 @@ int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap,
     return fail(h, BORN_ESTATE, "sinc tables missing");
   if (!h->src_levels_valid)
     return fail(h, BORN_ESTATE, "no source levels (run source_prop first)");
+  rc = ensure_tuned(h, kModeAdjoint);
+  if (rc) return rc;
   const size_t bytes = (size_t)h->n123 * 4;
   CK(h, cudaMemsetAsync(h->r0, 0, bytes, h->stream));
   CK(h, cudaMemsetAsync(h->r1, 0, bytes, h->stream));
@@ -641,6 +669,8 @@ int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out) {
   if (jt > h->jt_s || jt > h->jt_d)
     return fail(h, BORN_EINVAL, "jt %d exceeds the sinc tables' rows", jt);
   h->jt = jt;
+  rc = ensure_tuned(h, kModeForward);
+  if (rc) return rc;
   const size_t bytes = (size_t)h->n123 * 4;
   CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
   CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
@@ -696,6 +726,8 @@ int born_model(born_handle *h, int jt, int nt, float *traces_out) {
   if (!h->have_vel2) return fail(h, BORN_ESTATE, "vel2 not transferred");
   if (jt > h->jt_s || jt > h->jt_d)
     return fail(h, BORN_EINVAL, "jt %d exceeds the sinc tables' rows", jt);
+  rc = ensure_tuned(h, born::kModeModel);
+  if (rc) return rc;
   const size_t bytes = (size_t)h->n123 * 4;
   CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
   CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
@@ -732,6 +764,8 @@ int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
     return fail(h, BORN_ESTATE, "vel2 or model perturbation not transferred");
   if (jt > h->jt_s || jt > h->jt_d)
     return fail(h, BORN_EINVAL, "jt %d exceeds the sinc tables' rows", jt);
+  rc = ensure_tuned(h, born::kModeBornLin);
+  if (rc) return rc;
   const size_t bytes = (size_t)h->n123 * 4;
   CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
   CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
@@ -785,6 +819,9 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
   if (!h->have_vel2) return fail(h, BORN_ESTATE, "vel2 not transferred");
   if (jt > h->jt_s || jt > h->jt_d)
     return fail(h, BORN_EINVAL, "jt %d exceeds the sinc tables' rows", jt);
+  rc = ensure_tuned(h, born::kModeModel);
+  if (!rc) rc = ensure_tuned(h, born::kModeBornAdj);
+  if (rc) return rc;
   const size_t n = (size_t)h->n123, bytes = n * 4;
   const int nseg = (nt + interval - 1) / interval;
   rc = ensure_levels(h, &h->ckpt, &h->ckpt_levels, 2 * (size_t)nseg);
@@ -921,6 +958,30 @@ int born_synchronize(born_handle *h) {
 }
 
 int born_tile_config_count(void) { return born::tile_cfg_count(); }
+
+int born_autotune(born_handle *h, int enable) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  h->autotune = enable != 0;
+  for (int m = 0; m < 6; ++m) h->tuned_cfg[m] = -1;
+  if (!enable) return BORN_OK;
+  const int modes[] = {kModeSource, kModeForward, kModeAdjoint,
+                       born::kModeModel, born::kModeBornLin,
+                       born::kModeBornAdj};
+  for (int m : modes) {
+    rc = tune_mode(h, m);
+    if (rc) return rc;
+  }
+  return BORN_OK;
+}
+
+int born_tuned_config(const born_handle *h, int mode, int *cfg,
+                      float *ms_per_launch) {
+  if (!h || mode < 0 || mode > 5) return BORN_EINVAL;
+  if (cfg) *cfg = h->tile_cfg >= 0 ? h->tile_cfg : h->tuned_cfg[mode];
+  if (ms_per_launch) *ms_per_launch = h->tuned_ms[mode];
+  return BORN_OK;
+}
 
 int born_set_tiling(born_handle *h, int cfg, int zseg) {
   if (!h) return BORN_EINVAL;

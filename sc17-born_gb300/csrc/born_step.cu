@@ -86,31 +86,8 @@ __device__ __forceinline__ void set_comp(float4 &v, int j, float x) {
   else v.w = x;
 }
 
-// Reference summation order of cpuProp::prop (cpu_prop.cc:233-248):
-// ((((C0 p + CX1(..)) + CX2(..)) ... + CZ4(..)); v*S + p + p - old.
-// Intrinsics keep every multiply and add separately rounded.
-struct Nbr {
-  float x[8], y[8], z[8];  // [m-1] for -m, [4+m-1] for +m
-};
-
-__device__ __forceinline__ float stencil_sum(const float *c, float p,
-                                             const Nbr &n) {
-  float s = __fmul_rn(c[0], p);
-  s = __fadd_rn(s, __fmul_rn(c[2], __fadd_rn(n.x[0], n.x[4])));
-  s = __fadd_rn(s, __fmul_rn(c[5], __fadd_rn(n.x[1], n.x[5])));
-  s = __fadd_rn(s, __fmul_rn(c[8], __fadd_rn(n.x[2], n.x[6])));
-  s = __fadd_rn(s, __fmul_rn(c[11], __fadd_rn(n.x[3], n.x[7])));
-  s = __fadd_rn(s, __fmul_rn(c[3], __fadd_rn(n.y[0], n.y[4])));
-  s = __fadd_rn(s, __fmul_rn(c[6], __fadd_rn(n.y[1], n.y[5])));
-  s = __fadd_rn(s, __fmul_rn(c[9], __fadd_rn(n.y[2], n.y[6])));
-  s = __fadd_rn(s, __fmul_rn(c[12], __fadd_rn(n.y[3], n.y[7])));
-  s = __fadd_rn(s, __fmul_rn(c[1], __fadd_rn(n.z[0], n.z[4])));
-  s = __fadd_rn(s, __fmul_rn(c[4], __fadd_rn(n.z[1], n.z[5])));
-  s = __fadd_rn(s, __fmul_rn(c[7], __fadd_rn(n.z[2], n.z[6])));
-  s = __fadd_rn(s, __fmul_rn(c[10], __fadd_rn(n.z[3], n.z[7])));
-  return s;
-}
-
+// Leapfrog update of cpuProp::prop (cpu_prop.cc:233-248): v*S + p + p - old,
+// every operation separately rounded (no FMA contraction).
 __device__ __forceinline__ float leapfrog(float vel, float s, float p,
                                           float old) {
   return __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(vel, s), p), p), old);
@@ -129,6 +106,7 @@ __device__ __forceinline__ float point_value(const PointSet &ps, int idx) {
 // gy, plane z, in point order.  Uniform early-out when the plane is empty.
 __device__ __forceinline__ void inject_row(const PointSet &ps, int n1, int n2,
                                            int z, int gy, int gx, float4 &v) {
+  if (z < ps.zlo || z > ps.zhi) return;
   const int off = ps.plane_off[z];
   if (off < 0) return;
   const int4 h = *reinterpret_cast<const int4 *>(ps.cell_head + off +
@@ -151,6 +129,7 @@ __device__ __forceinline__ void inject_row(const PointSet &ps, int n1, int n2,
 __device__ __forceinline__ void extract_row(const PointSet &ps, int n1, int n2,
                                             int z, int gy, int gx,
                                             const float4 &v) {
+  if (z < ps.zlo || z > ps.zhi) return;
   const int off = ps.plane_off[z];
   if (off < 0) return;
   const int4 h = *reinterpret_cast<const int4 *>(ps.cell_head + off +
@@ -174,22 +153,54 @@ __device__ __forceinline__ void st4(float *p, const float4 &v) {
   *reinterpret_cast<float4 *>(p) = v;
 }
 
-// Gathers the x/y neighbours of cell j from a TMA box; z from the window.
+// Stencil sums of this thread's 4 consecutive cells (x .. x+3) of one row,
+// from a TMA box (x/y neighbours) and the register z window.  Each cell's
+// sum is formed in the reference order of cpuProp::prop (cpu_prop.cc:235-247):
+// C0 p, then the x pairs, the y pairs and the z pairs, every product and sum
+// separately rounded; the four cells advance together so that every shared
+// load is a float4 (3 for the x window, 2 per y offset).
 template <int BX>
-__device__ __forceinline__ void gather(const float *box, int brow, int bcol,
-                                       const float4 (&q)[9], int j, Nbr &n,
-                                       float &center) {
-  const float *r = box + brow * BX + bcol;  // points at x (j = 0)
+__device__ __forceinline__ float4 stencil4(const float *box, int brow,
+                                           int bcol, const float4 (&q)[9],
+                                           const float *c, float4 &center) {
+  const float *r = box + brow * BX + bcol;
+  float w[12];
+  {
+    const float4 L = *reinterpret_cast<const float4 *>(r - 4);
+    const float4 M = *reinterpret_cast<const float4 *>(r);
+    const float4 R = *reinterpret_cast<const float4 *>(r + 4);
+    w[0] = L.x; w[1] = L.y; w[2] = L.z; w[3] = L.w;
+    w[4] = M.x; w[5] = M.y; w[6] = M.z; w[7] = M.w;
+    w[8] = R.x; w[9] = R.y; w[10] = R.z; w[11] = R.w;
+    center = M;
+  }
+  float s[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    s[j] = __fmul_rn(c[0], w[4 + j]);
+    s[j] = __fadd_rn(s[j], __fmul_rn(c[2], __fadd_rn(w[3 + j], w[5 + j])));
+    s[j] = __fadd_rn(s[j], __fmul_rn(c[5], __fadd_rn(w[2 + j], w[6 + j])));
+    s[j] = __fadd_rn(s[j], __fmul_rn(c[8], __fadd_rn(w[1 + j], w[7 + j])));
+    s[j] = __fadd_rn(s[j], __fmul_rn(c[11], __fadd_rn(w[0 + j], w[8 + j])));
+  }
+  const int cy[4] = {3, 6, 9, 12}, cz[4] = {1, 4, 7, 10};
 #pragma unroll
   for (int m = 1; m <= 4; ++m) {
-    n.x[m - 1] = r[j - m];
-    n.x[4 + m - 1] = r[j + m];
-    n.y[m - 1] = r[j - m * BX];
-    n.y[4 + m - 1] = r[j + m * BX];
-    n.z[m - 1] = comp(q[4 - m], j);
-    n.z[4 + m - 1] = comp(q[4 + m], j);
+    const float4 u = *reinterpret_cast<const float4 *>(r - m * BX);
+    const float4 d = *reinterpret_cast<const float4 *>(r + m * BX);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      s[j] = __fadd_rn(s[j], __fmul_rn(c[cy[m - 1]],
+                                       __fadd_rn(comp(u, j), comp(d, j))));
   }
-  center = r[j];
+#pragma unroll
+  for (int m = 1; m <= 4; ++m)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      s[j] = __fadd_rn(
+          s[j], __fmul_rn(c[cz[m - 1]],
+                          __fadd_rn(comp(q[4 - m], j), comp(q[4 + m], j))));
+  return make_float4(s[0], s[1], s[2], s[3]);
 }
 
 // ---------------------------------------------------------------------------
@@ -369,7 +380,9 @@ __global__ void __launch_bounds__(Tile<TX, TY>::kThreads)
       if (MODE == kModeAdjoint && PB && p.pb.active && valid && ok)
         inject_row(p.pb, n1, n2, zo, gy, gx, ob);
 
-      float4 na = oa, nb = ob, ga = zero4;
+      float4 na = oa, nb = ob, ga = zero4, sb = zero4, ca = zero4, cb = zero4;
+      if (M::kBoxA) ga = stencil4<BX>(box_a, brow, bcol, qa, p.c, ca);
+      if (M::kBoxB) sb = stencil4<BX>(box_b, brow, bcol, qb, p.c, cb);
       float bj[4];
 #pragma unroll
       for (int jj = 0; jj < 4; ++jj) {
@@ -377,14 +390,9 @@ __global__ void __launch_bounds__(Tile<TX, TY>::kThreads)
         const float b = (e >= 0 && e < kNBound) ? s_bound[e] : 1.0f;
         bj[jj] = b;
         if (M::kBoxA) {
-          Nbr n;
-          float c;
-          gather<BX>(box_a, brow, bcol, qa, jj, n, c);
           float old = comp(oa, jj);
           if (M::kDampA) old = __fmul_rn(old, b);
-          const float sa = stencil_sum(p.c, c, n);
-          set_comp(ga, jj, sa);
-          float v = leapfrog(comp(va, jj), sa, c, old);
+          float v = leapfrog(comp(va, jj), comp(ga, jj), comp(ca, jj), old);
           // the adjoint of the linearised step injects its data before the
           // taper (see below); every other tapered mode tapers here
           if (MODE != kModeBornAdj && M::kDampA) v = __fmul_rn(v, b);
@@ -394,12 +402,9 @@ __global__ void __launch_bounds__(Tile<TX, TY>::kThreads)
           set_comp(na, jj, __fmul_rn(__fmul_rn(comp(oa, jj), b), b));
         }
         if (M::kBoxB) {
-          Nbr n;
-          float c;
-          gather<BX>(box_b, brow, bcol, qb, jj, n, c);
           float old = comp(ob, jj);
           if (M::kDampB) old = __fmul_rn(old, b);
-          float v = leapfrog(comp(vb, jj), stencil_sum(p.c, c, n), c, old);
+          float v = leapfrog(comp(vb, jj), comp(sb, jj), comp(cb, jj), old);
           // linearised Born: scattering source m (A s) inside the taper
           if (MODE == kModeBornLin)
             v = __fadd_rn(v, __fmul_rn(comp(im, jj), comp(ga, jj)));

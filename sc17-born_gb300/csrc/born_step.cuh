@@ -58,6 +58,7 @@ struct PointSet {
   float *traces;          // [npts][nt_trace]
   int npts;
   int nt_trace;
+  int zlo, zhi;           // planes holding points (skip the lookup elsewhere)
   int id;                 // first trace sample used this step
   int active;             // reference guard: id + 7 < nt_trace
   float scale;            // dir / jt for injection, unused for extraction
@@ -86,8 +87,8 @@ struct StepParams {
 };
 
 constexpr unsigned int kErrWaitTimeout = 1u;
-constexpr int kStages = 8;   // box ring depth (planes)
-constexpr int kCStages = 4;  // centre ring depth (output planes)
+constexpr int kStages = 7;   // box ring depth (planes): 5 resident + 2 ahead
+constexpr int kCStages = 3;  // centre ring depth (output planes): 2 ahead
 
 struct StepMaps {
   CUtensorMap box_a, box_b;       // halo boxes of the current levels
