@@ -222,6 +222,23 @@ int born_dot_f64(born_op *op, const float *a, const float *b, long long n,
 int born_cg_solve(born_op *op, const float *data, float *model, int niter,
                   double *resid);
 
+/* FP64 dot product that allocates nothing.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory where they need
+ * a dot product: applications whose GPU memory is all owned by their own
+ * pool, and code that keeps other streams busy and cannot take the
+ * device-wide synchronisation of cudaMalloc/cudaFree.  a, b: device float
+ * vectors of n elements on the current device; out: host double; stream: a
+ * cudaStream_t (null for the default stream); the call waits for the result.
+ * Its scratch is a fixed file-scope device array of 65536 partial sums
+ * (512 KiB, held by every GPU that loads the library until exit), so n is
+ * limited to BORN_DOT_NOALLOC_MAX elements; larger n returns BORN_EINVAL.
+ * All calls share that array: calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's address on that device; make it
+ * before any stream capture begins. */
+#define BORN_DOT_NOALLOC_MAX 268435456LL
+int born_dot_f64_noalloc(const float *a, const float *b, long long n,
+                         double *out, void *stream);
+
 /* Tuning: tile configuration index (0..born_tile_config_count()-1, or -1 for
  * the built-in choice) and z-segment depth (0 = automatic). */
 int born_tile_config_count(void);

@@ -96,6 +96,8 @@ _SIGS = {
                                C.POINTER(C.c_double)]),
     "born_cg_solve": (C.c_int, [_vp, _vp, _vp, C.c_int,
                                 C.POINTER(C.c_double)]),
+    "born_dot_f64_noalloc": (C.c_int, [_vp, _vp, C.c_longlong,
+                                       C.POINTER(C.c_double), _vp]),
     # host geometry (csrc/born_host.h)
     "born_sinc_table": (C.c_int, [C.c_int, C.c_int, _fp]),
     "born_calc_stability": (C.c_float, [C.c_float, C.c_float, C.c_float,

@@ -18,7 +18,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libborn_gb300.so")
 
-SOURCES = ["born_step.cu", "born_api.cu", "born_operator.cu", "born_host.cc"]
+SOURCES = ["born_step.cu", "born_api.cu", "born_operator.cu", "born_noalloc.cu",
+           "born_host.cc"]
 HEADERS = ["born_step.cuh", "born_host.h", "born_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
