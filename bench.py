@@ -148,14 +148,27 @@ def dist_env():
 
 
 def barrier_max(value: float, world: int) -> float:
+    """Max of a per-rank value over all ranks (after a barrier)."""
     if world <= 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.barrier()
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def shot_of_rank(rank: int, nshots: int) -> int:
+    """Shots are independent: rank r runs shot r (modulo the shot count)."""
+    return rank % max(1, nshots)
+
+
+def aggregate_rate(cells_per_rank: float, steps: int, t_ms_max: float,
+                   world: int) -> float:
+    """Whole-job Gcell-updates/s: all ranks' cells over the slowest rank."""
+    return world * cells_per_rank * steps / (t_ms_max / 1e3) / 1e9
 
 
 # ---------------------------------------------------------------------------
@@ -245,7 +258,8 @@ def run_gpu_arm(args):
     born = package()
     born.lib()
     wl = workload_module()
-    case = wl.prepare_shot(born, args.config, nt=args.nt, n=args.model_n)
+    case = wl.prepare_shot(born, args.config, nt=args.nt, n=args.model_n,
+                           shot=shot_of_rank(rank, 48))
     nz, ny, nx = case["shape"]
     nt, jt = case["nt"], case["jts"]
     n_int = wl.interior_cells(case["shape"])
@@ -299,12 +313,16 @@ def run_gpu_arm(args):
         prop.synchronize()
         torch.cuda.synchronize()
     launches = prop.launches - launches0
+    tiles = {}
+    for mode, name in ((1, "forward"), (0, "source"), (2, "adjoint")):
+        cfg, ms = prop.tuned_config(mode)
+        tiles[name] = cfg
     t_ms = start.elapsed_time(stop)
     t_ms = barrier_max(t_ms, world)
     fwd_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
     src_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
     adj_ms = sum(e[2].elapsed_time(e[3]) for e in evs) / args.steps
-    value = world * cells_per_step * args.steps / (t_ms / 1e3) / 1e9
+    value = aggregate_rate(cells_per_step, args.steps, t_ms, world)
 
     # roofline of the dominant kernel: the fused RTM adjoint step
     peak, peak_kind = measured_peak()
@@ -350,7 +368,7 @@ def run_gpu_arm(args):
                        "l2": "inputs larger than L2 (7 x %.0f MB fields)" %
                              (nx * ny * nz * 4 / 1e6),
                        "parallelism": f"shots x{world} (one per GPU)"},
-            "roofline": roofline, "phases": phases,
+            "roofline": roofline, "phases": phases, "tile_cfg": tiles,
             "clocks": clk.summary(), "gpu_launches": launches,
             "e2e": e2e, "cpu_baseline": cpu,
         }

@@ -294,6 +294,8 @@ int launch(born_handle *h, int mode, bool pa, bool pb, const float *a_cur,
   const float *any = h->vel2;  // any valid grid buffer for unused slots
   int rc = get_map(h, a_cur ? a_cur : any, cfg, 0, &maps.box_a);
   if (!rc) rc = get_map(h, b_cur ? b_cur : any, cfg, 0, &maps.box_b);
+  if (!rc) rc = get_map(h, a_cur ? a_cur : any, cfg, 1, &maps.zc_a);
+  if (!rc) rc = get_map(h, b_cur ? b_cur : any, cfg, 1, &maps.zc_b);
   const unsigned mask = born::centre_mask(mode, pa, pb);
   for (int sl = 0; sl < born::kNumCentre && !rc; ++sl) {
     const bool used = mask & (1u << sl);

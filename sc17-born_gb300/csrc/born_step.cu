@@ -252,14 +252,18 @@ __global__ void __launch_bounds__(Tile<TX, TY>::kThreads)
   constexpr uint32_t kBoxBytes = T::kBoxFloats * 4u;
   constexpr uint32_t kCBytes = T::kCFloats * 4u;
   extern __shared__ __align__(128) float smem_raw[];
-  __shared__ __align__(8) uint64_t bars[kStages];
-  __shared__ __align__(8) uint64_t cbars[kCStages];
+  __shared__ __align__(8) uint64_t zbars[kZStages];
+  __shared__ __align__(8) uint64_t obars[kOStages];
   __shared__ int abort_flag;
   __shared__ float s_bound[kNBound];
   // TMA destinations need 128-byte alignment: align the dynamic base here
   // (the launch reserves 128 spare bytes for this)
   float *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u) / 4u;
-  float *cring = smem + kStages * NF * PITCH;
+  // z ring: centre tiles of the current levels, one per new plane
+  float *zring = smem;
+  // output ring: halo boxes and per-cell inputs of the output plane
+  constexpr int OSTRIDE = NF * PITCH + NC * CF;
+  float *oring = smem + kZStages * NF * CF;
 
   const int tid = threadIdx.x;
   const int lx = tid % (TX / 4), ly = tid / (TX / 4);
@@ -283,8 +287,8 @@ __global__ void __launch_bounds__(Tile<TX, TY>::kThreads)
   }
 
   if (tid == 0) {
-    for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
-    for (int s = 0; s < kCStages; ++s) mbar_init(&cbars[s], 1);
+    for (int s = 0; s < kZStages; ++s) mbar_init(&zbars[s], 1);
+    for (int s = 0; s < kOStages; ++s) mbar_init(&obars[s], 1);
     // a wait elsewhere already gave up: the whole CTA leaves untouched
     abort_flag = *reinterpret_cast<volatile unsigned int *>(p.err) != 0u;
     mbar_fence_init();
@@ -293,34 +297,40 @@ __global__ void __launch_bounds__(Tile<TX, TY>::kThreads)
   __syncthreads();
   if (abort_flag) return;  // uniform: read after the barrier
 
-  const int K = (z1 - z0) + 2 * kRadius;  // box planes z0-4 .. z1+3
+  const int K = (z1 - z0) + 2 * kRadius;  // z-window planes z0-4 .. z1+3
   const int J = z1 - z0;                  // output planes
-  auto issue_box = [&](int k) {
+  auto issue_z = [&](int k) {
     const int plane = z0 - kRadius + k;
-    const int st = k % kStages;
-    mbar_expect_tx(&bars[st], NF * kBoxBytes);
-    float *dst = smem + st * NF * PITCH;
+    const int st = k % kZStages;
+    mbar_expect_tx(&zbars[st], NF * kCBytes);
+    float *dst = zring + st * NF * CF;
+    if (M::kBoxA) tma_load_3d(dst, &maps.zc_a, x0, y0, plane, &zbars[st]);
+    if (M::kBoxB)
+      tma_load_3d(dst + (M::kBoxA ? CF : 0), &maps.zc_b, x0, y0, plane,
+                  &zbars[st]);
+  };
+  auto issue_out = [&](int j) {
+    const int plane = z0 + j;
+    const int st = j % kOStages;
+    mbar_expect_tx(&obars[st], NF * kBoxBytes + NC * kCBytes);
+    float *dst = oring + st * OSTRIDE;
     if (M::kBoxA)
       tma_load_3d(dst, &maps.box_a, x0 - kRadius, y0 - kRadius, plane,
-                  &bars[st]);
+                  &obars[st]);
     if (M::kBoxB)
       tma_load_3d(dst + (M::kBoxA ? PITCH : 0), &maps.box_b, x0 - kRadius,
-                  y0 - kRadius, plane, &bars[st]);
-  };
-  auto issue_centre = [&](int j) {
-    const int st = j % kCStages;
-    mbar_expect_tx(&cbars[st], NC * kCBytes);
-    float *dst = cring + st * NC * CF;
+                  y0 - kRadius, plane, &obars[st]);
+    float *cdst = dst + NF * PITCH;
 #pragma unroll
     for (int s = 0; s < kNumCentre; ++s)
       if (M::kMask & (1u << s))
-        tma_load_3d(dst + M::pos(s) * CF, &maps.cm[s], x0, y0, z0 + j,
-                    &cbars[st]);
+        tma_load_3d(cdst + M::pos(s) * CF, &maps.cm[s], x0, y0, plane,
+                    &obars[st]);
   };
   if (tid == 0) {
     if (NF > 0)
-      for (int k = 0; k < min(K, kStages); ++k) issue_box(k);
-    for (int j = 0; j < min(J, kCStages); ++j) issue_centre(j);
+      for (int k = 0; k < min(K, kZStages); ++k) issue_z(k);
+    for (int j = 0; j < min(J, kOStages); ++j) issue_out(j);
   }
 
   float4 qa[9], qb[9];
@@ -333,32 +343,31 @@ __global__ void __launch_bounds__(Tile<TX, TY>::kThreads)
   const int coff = ly * TX + 4 * lx;  // this thread's float4 in a centre tile
 
   for (int k = 0; k < K; ++k) {
-    const int st = k % kStages;
+    const int st = k % kZStages;
     const int j = k - 2 * kRadius;       // output index once k >= 8
     const int zo = z0 + j;
     const long long idx = (long long)zo * n12 + (long long)gy * n1 + gx;
 
     bool ok = true;
     if (NF > 0) {
-      ok = mbar_wait_bounded(&bars[st], (uint32_t)((k / kStages) & 1));
+      ok = mbar_wait_bounded(&zbars[st], (uint32_t)((k / kZStages) & 1));
       // newest plane's centre enters the z window
-      const float *sa = smem + st * NF * PITCH;
+      const float *sa = zring + st * NF * CF + coff;
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         qa[i] = qa[i + 1];
         qb[i] = qb[i + 1];
       }
-      if (M::kBoxA)
-        qa[8] = *reinterpret_cast<const float4 *>(sa + brow * BX + bcol);
+      if (M::kBoxA) qa[8] = *reinterpret_cast<const float4 *>(sa);
       if (M::kBoxB)
-        qb[8] = *reinterpret_cast<const float4 *>(
-            sa + (M::kBoxA ? PITCH : 0) + brow * BX + bcol);
+        qb[8] = *reinterpret_cast<const float4 *>(sa + (M::kBoxA ? CF : 0));
     }
 
     if (j >= 0 && ok) {
-      const int cs = j % kCStages;
-      ok = mbar_wait_bounded(&cbars[cs], (uint32_t)((j / kCStages) & 1));
-      const float *cst = cring + cs * NC * CF + coff;
+      const int os = j % kOStages;
+      ok = mbar_wait_bounded(&obars[os], (uint32_t)((j / kOStages) & 1));
+      const float *ost = oring + os * OSTRIDE;
+      const float *cst = ost + NF * PITCH + coff;
       auto centre = [&](int slot) {
         return *reinterpret_cast<const float4 *>(cst + M::pos(slot) * CF);
       };
@@ -371,8 +380,7 @@ __global__ void __launch_bounds__(Tile<TX, TY>::kThreads)
                                                                         : zero4;
       const float4 im = (M::kMask & (1u << kImg)) ? centre(kImg) : zero4;
 
-      const int so = (k - kRadius) % kStages;  // stage of the output plane
-      const float *box_a = smem + so * NF * PITCH;
+      const float *box_a = ost;
       const float *box_b = box_a + (M::kBoxA ? PITCH : 0);
       const int ez = min(zo - 4, n3 - 4 - zo);
 
@@ -473,16 +481,15 @@ __global__ void __launch_bounds__(Tile<TX, TY>::kThreads)
     if (abort_flag) break;
     if (tid == 0) {
       fence_proxy_async();
-      if (NF > 0 && k >= kRadius && k - kRadius + kStages < K)
-        issue_box(k - kRadius + kStages);
-      if (j >= 0 && j + kCStages < J) issue_centre(j + kCStages);
+      if (NF > 0 && k + kZStages < K) issue_z(k + kZStages);
+      if (j >= 0 && j + kOStages < J) issue_out(j + kOStages);
     }
   }
 
   if (abort_flag && tid == 0) {
     // drain whatever is still in flight (bounded) before the CTA retires
-    for (int s = 0; s < kStages + kCStages; ++s) {
-      uint64_t *b = s < kStages ? &bars[s] : &cbars[s - kStages];
+    for (int s = 0; s < kZStages + kOStages; ++s) {
+      uint64_t *b = s < kZStages ? &zbars[s] : &obars[s - kZStages];
       const uint64_t t0 = global_ns();
       while (!mbar_try_wait(b, 0) && !mbar_try_wait(b, 1) &&
              global_ns() - t0 < 100000000ull) {
@@ -518,8 +525,9 @@ template <int MODE, bool PA, bool PB, int TX, int TY>
 size_t smem_bytes_t() {
   using M = ModeTraits<MODE, PA, PB>;
   using T = Tile<TX, TY>;
-  return (size_t)kStages * M::kNF * T::kBoxPitch * 4 +
-         (size_t)kCStages * M::kNC * T::kCFloats * 4 + 128;
+  return (size_t)kZStages * M::kNF * T::kCFloats * 4 +
+         (size_t)kOStages * (M::kNF * T::kBoxPitch + M::kNC * T::kCFloats) * 4 +
+         128;
 }
 
 template <int MODE, bool PA, bool PB, int TX, int TY>

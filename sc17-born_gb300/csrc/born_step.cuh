@@ -4,13 +4,17 @@
 // the interior [4, n-4)^3 of a [n3][n2][n1] float grid (n1 fastest).  Work is
 // split into xy tiles (TX x TY cells) and z segments; each CTA marches its
 // segment plane by plane.  All HBM reads are asynchronous TMA copies
-// (cp.async.bulk.tensor.3d) completing on mbarriers:
-//   * box ring: the current level of every propagated field, one
-//     (TX+8) x (TY+8) box per plane, kStages deep; x/y neighbours come from
-//     the box, the 9-plane z window is kept in registers;
-//   * centre ring: the per-cell inputs of the output plane (previous levels,
-//     velocities, image or reflectivity), one TX x TY tile each, kCStages
-//     deep.
+// (cp.async.bulk.tensor.3d) completing on mbarriers, in two small rings:
+//   * z ring (kZStages): the TX x TY centre tile of every propagated field's
+//     current level for each new plane; its values enter the 9-plane z window
+//     kept in registers;
+//   * output ring (kOStages): for the plane being written, the
+//     (TX+8) x (TY+8) halo box of every propagated field (x/y neighbours) and
+//     the per-cell inputs (previous levels, velocities, image or
+//     reflectivity), one TX x TY tile each.
+// A plane's centre is thus read twice (z ring, then inside its box four
+// planes later, from L2), which keeps the shared memory per CTA small enough
+// for three 128-thread CTAs per SM.
 // The new level (and the image) are written once with float4 stores, so HBM
 // sees the compulsory bytes only.
 //
@@ -87,11 +91,12 @@ struct StepParams {
 };
 
 constexpr unsigned int kErrWaitTimeout = 1u;
-constexpr int kStages = 7;   // box ring depth (planes): 5 resident + 2 ahead
-constexpr int kCStages = 3;  // centre ring depth (output planes): 2 ahead
+constexpr int kZStages = 3;  // z-window ring depth (new planes, 2 ahead)
+constexpr int kOStages = 3;  // output ring depth (output planes, 2 ahead)
 
 struct StepMaps {
   CUtensorMap box_a, box_b;       // halo boxes of the current levels
+  CUtensorMap zc_a, zc_b;         // centre tiles of the current levels
   CUtensorMap cm[kNumCentre];     // centre tiles, by CentreSlot
 };
 

@@ -89,8 +89,10 @@ CONFIGS = {
 
 
 def prepare_shot(born, name: str = "c2", nt: int | None = None,
-                 n: int | None = None, nbound: int | None = None) -> dict:
-    """Propagator inputs for one shot of configuration ``name``."""
+                 n: int | None = None, nbound: int | None = None,
+                 shot: int = 0) -> dict:
+    """Propagator inputs for shot ``shot`` of configuration ``name`` (shot 0
+    at the model centre, others offset along x on a 20 m lattice)."""
     cfg = dict(CONFIGS[name])
     if n is not None:
         cfg["n"] = n
@@ -111,7 +113,8 @@ def prepare_shot(born, name: str = "c2", nt: int | None = None,
     nt_big = nt_data + 8
     wav = born.wavelet_deriv(ricker(nt_data, dt_data, cfg["f"]), dt_data)
     mid = (n // 2) * d
-    locs_s, src = born.source_geometry(mid, mid, cfg["src_depth"], o, dd, nc,
+    sx = mid + 20.0 * (((shot * 7) % 11) - 5 if shot else 0)
+    locs_s, src = born.source_geometry(sx, mid, cfg["src_depth"], o, dd, nc,
                                        nc, wav, nt_big)
     seed = int(locs_s[3] % 10000)
     shape = (nc, nc, nc)

@@ -1,0 +1,51 @@
+"""The multi-rank path of bench.py on CPU ranks (gloo, world size 2): shots
+are sharded one per rank with no data-path collective, and the reported
+time is the maximum over ranks, so the whole-job rate counts every rank's
+cells against the slowest rank."""
+import os
+import socket
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _worker(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port),
+                      RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import importlib.util
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location(
+        "bench_mod", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    r, w, local = bench.dist_env()
+    t_ms = 100.0 + 50.0 * r  # rank 1 is slower
+    t_max = bench.barrier_max(t_ms, w)
+    rate = bench.aggregate_rate(1e9, 2, t_max, w)
+    out[r] = (bench.shot_of_rank(r, 48), t_max, rate)
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_shard_shots_and_take_max_time():
+    world = 2
+    port = _free_port()
+    with mp.Manager() as m:
+        out = m.dict()
+        mp.spawn(_worker, args=(world, port, out), nprocs=world, join=True)
+        res = dict(out)
+    assert res[0][0] == 0 and res[1][0] == 1          # one shot per rank
+    assert res[0][1] == res[1][1] == 150.0             # max over ranks
+    assert abs(res[0][2] - 2 * 1e9 * 2 / 0.150 / 1e9) < 1e-9  # weak scaling
