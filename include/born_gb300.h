@@ -130,6 +130,20 @@ int born_set_receiver_func(born_handle *h, int rec_nx, int rec_ny, int nt_big,
 /* slot 1: random-boundary model (vel1), slot 2: plain model (vel2) */
 int born_set_velocity(born_handle *h, int slot, int nx, int ny, int nz,
                       const float *v2dt2);
+/* Velocity slot (1 or 2) made on the device from a model velocity (host,
+ * vn3 x vn2 x vn1 m/s, origin vo, spacing vd): vel_fd_3d::rand_subspace
+ * (vel_fd_3d.cc:29-134) with a counter-based generator (SplitMix64 of seed,
+ * cell and draw) instead of rand(), so the random boundary is deterministic;
+ * cells outside the nrand bands equal born_rand_subspace's bit for bit.  At
+ * most 64 draws per cell (the reference loops until one is accepted).
+ * (o, d) describe the compute grid; output is v^2 dt^2. */
+int born_make_velocity(born_handle *h, int slot, const float *vel, int vn1,
+                       int vn2, int vn3, float vo1, float vo2, float vo3,
+                       float vd1, float vd2, float vd3, float vmax,
+                       unsigned long long seed, int nrand1, int nrand2,
+                       int nrand3, float dt, float o1, float o2, float o3,
+                       float d1, float d2, float d3);
+int born_get_velocity(born_handle *h, int slot, float *out);
 /* Reflectivity for the Born forward (the image the forward reads). */
 int born_set_reflectivity(born_handle *h, const float *img);
 

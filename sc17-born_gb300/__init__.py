@@ -67,6 +67,11 @@ _SIGS = {
     "born_set_velocity": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, C.c_int,
                                     _fp]),
     "born_set_reflectivity": (C.c_int, [_vp, _fp]),
+    "born_make_velocity": (C.c_int, [_vp, C.c_int, _fp, C.c_int, C.c_int,
+                                     C.c_int] + [C.c_float] * 7 +
+                           [C.c_ulonglong, C.c_int, C.c_int, C.c_int] +
+                           [C.c_float] * 7),
+    "born_get_velocity": (C.c_int, [_vp, C.c_int, _fp]),
     "born_source_prop": (C.c_int, [_vp, C.c_int, C.c_int, _fp, _fp]),
     "born_rtm_adjoint": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _fp]),
     "born_rtm_forward": (C.c_int, [_vp, C.c_int, C.c_int, _fp]),
@@ -128,6 +133,9 @@ _SIGS = {
                                    C.c_int]),
     "born_add_image": (C.c_int, [_fp, C.c_int, C.c_int, C.c_int, _fp, C.c_int,
                                  C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "born_sep_read_info": (C.c_int, [C.c_char_p, _vp]),
+    "born_sep_read": (C.c_int, [C.c_char_p, _fp, C.c_longlong]),
+    "born_sep_write": (C.c_int, [C.c_char_p, _vp, _fp, C.c_int]),
 }
 
 _lib = None
@@ -317,6 +325,20 @@ class Gb300Prop(Handle):
         self.check(self.lib.born_rtm_forward(self.h, jt, nt, fptr(target)))
         if rec is not None and target is not rec:
             rec[...] = target
+
+    def make_velocity(self, slot, vel, vo, vd, vmax, seed, nrand, dt, o, d):
+        """vel_fd_3d::rand_subspace on the device (counter-based draws)."""
+        vel = f32(vel)
+        vn3, vn2, vn1 = vel.shape
+        self.check(self.lib.born_make_velocity(
+            self.h, slot, fptr(vel), vn1, vn2, vn3, vo[0], vo[1], vo[2],
+            vd[0], vd[1], vd[2], vmax, seed, nrand[0], nrand[1], nrand[2], dt,
+            o[0], o[1], o[2], d[0], d[1], d[2]))
+
+    def get_velocity(self, slot):
+        out = np.empty(self.shape, np.float32)
+        self.check(self.lib.born_get_velocity(self.h, slot, fptr(out)))
+        return out
 
     # ---- device-resident variants (no host round trips) ----
     def source_prop_device(self, jts, nt):
@@ -523,3 +545,39 @@ def rand_subspace(vel, vo, vd, vmax, irand, nrand, dt, shape, o, d):
                                  nrand[1], nrand[2], dt, n1, n2, n3, o[0],
                                  o[1], o[2], d[0], d[1], d[2], fptr(out)))
     return out
+
+
+# ---------------------------------------------------------------------------
+# SEP regular files (csrc/born_sepio.cc)
+
+class SepInfo(C.Structure):
+    _fields_ = [("ndim", C.c_int), ("n", C.c_longlong * 6),
+                ("o", C.c_float * 6), ("d", C.c_float * 6),
+                ("big_endian", C.c_int), ("in_", C.c_char * 1024)]
+
+
+def read_sep(path: str):
+    """Reads a SEP regular file; returns (array, o, d).  The array has the
+    header's axes reversed (n1 fastest), e.g. [n3, n2, n1] for a cube."""
+    info = SepInfo()
+    _ck(lib().born_sep_read_info(path.encode(), C.byref(info)))
+    shape = tuple(int(info.n[a]) for a in range(max(info.ndim, 1)))
+    out = np.empty(int(np.prod(shape)), np.float32)
+    _ck(lib().born_sep_read(path.encode(), fptr(out), out.size))
+    k = max(info.ndim, 1)
+    return (out.reshape(shape[::-1]), tuple(info.o[:k]), tuple(info.d[:k]))
+
+
+def write_sep(path: str, array, o=None, d=None, big_endian: bool = True):
+    """Writes a SEP regular file (path and path + '@'); axis 1 is the
+    array's last (fastest) axis."""
+    a = f32(array)
+    shape = a.shape[::-1]
+    info = SepInfo()
+    info.ndim = len(shape)
+    for i, n in enumerate(shape):
+        info.n[i] = n
+        info.o[i] = 0.0 if o is None else o[i]
+        info.d[i] = 1.0 if d is None else d[i]
+    _ck(lib().born_sep_write(path.encode(), C.byref(info), fptr(a),
+                             int(big_endian)))

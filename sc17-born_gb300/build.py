@@ -19,7 +19,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libborn_gb300.so")
 
 SOURCES = ["born_step.cu", "born_api.cu", "born_operator.cu", "born_noalloc.cu",
-           "born_host.cc"]
+           "born_velocity.cu", "born_host.cc", "born_sepio.cc"]
 HEADERS = ["born_step.cuh", "born_host.h", "born_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -83,6 +83,23 @@ int born_extract_sub(const float *whole, int w1, int w2, int w3, float *sub,
 int born_add_image(float *whole, int w1, int w2, int w3, const float *sub,
                    int s1, int s2, int s3, int f1, int f2, int f3);
 
+/* SEP regular files (the reference's genericIO datasets): header text of
+ * key=value pairs (n1..n6, o1..o6, d1..d6, esize=4, data_format xdr_float or
+ * native_float, in= binary path, relative to the header's folder). */
+typedef struct {
+  int ndim;            /* highest axis given in the header */
+  long long n[6];
+  float o[6], d[6];
+  int big_endian;      /* 1 for xdr_float */
+  char in[1024];       /* resolved path of the binary data */
+} born_sep_info;
+int born_sep_read_info(const char *header, born_sep_info *info);
+/* count must equal n1*...*n6 of the header */
+int born_sep_read(const char *header, float *out, long long count);
+/* writes header and header@ (binary), big_endian selects xdr_float */
+int born_sep_write(const char *header, const born_sep_info *info,
+                   const float *data, int big_endian);
+
 #ifdef __cplusplus
 }
 #endif
