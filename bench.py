@@ -453,13 +453,198 @@ def e2e_measure(born, case, args, dev, cells_per_step, world):
             "api": "gpu_funcs_3d.h entry points, pinned host buffers"}
 
 
+def run_batched(args):
+    """c4: batched multi-shot RTM (source propagation + adjoint of every
+    shot, one launch per step for all shots, time loops as CUDA graphs)
+    against the same shots run one after another."""
+    import torch
+    born = package()
+    born.lib()
+    wl = workload_module()
+    nt = args.nt if args.nt else 2500
+    t0 = time.perf_counter()
+    shots, com = wl.prepare_batch_c4(born, nshots=args.shots, nt=nt)
+    for h in shots:
+        h.set_storage(args.storage)
+    setup_s = time.perf_counter() - t0
+    jt, ntf = com["jt"], com["nt"]
+    cells = sum(wl.interior_cells(h.shape) for h in shots)
+    batch = born.Batch(shots, graph=not args.no_graph)
+    stream = torch.cuda.ExternalStream(batch.stream)
+
+    def rtm_all():
+        batch.source_prop(jt, ntf)
+        batch.rtm_adjoint(jt, ntf)
+
+    for _ in range(args.warmup):
+        rtm_all()
+    batch.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            rtm_all()
+        e1.record(stream)
+        batch.synchronize()
+    t_b = e0.elapsed_time(e1) / args.steps
+    # the same shots one after another through the single-shot loops
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    for h in shots:
+        # tile autotuning of each shot's own grid happens outside the timing
+        h.source_prop_device(jt, 1)
+        h.rtm_adjoint_device(jt, 1, swap=1)
+        h.synchronize()
+    torch.cuda.synchronize()
+    t_s = 0.0
+    for h in shots:
+        st = torch.cuda.ExternalStream(h.stream)
+        e2.record(st)
+        h.source_prop_device(jt, ntf)
+        h.rtm_adjoint_device(jt, ntf, swap=1)
+        e3.record(st)
+        h.synchronize()
+        t_s += e2.elapsed_time(e3)
+    # RTM = source propagation + adjoint (two fields) per step
+    cu = cells * ntf * 2
+    line = {"metric": "Gcell-updates/s batched RTM (c4)",
+            "value": round(cu / (t_b / 1e3) / 1e9, 3),
+            "unit": "Gcell-updates/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(t_b, 2),
+            "higher_is_better": True,
+            "dtype": "f32 arithmetic; levels " + args.storage,
+            "data": "synthetic (seeded, shapes of the config)",
+            "config": {"workload": f"c4: {len(shots)} shots, apertures "
+                       "192..320 x 192..320 x 256..400 on 800x800x400 at "
+                       f"10 m, nt={ntf}", "graph": not args.no_graph},
+            "shot_steps_per_s": round(len(shots) * ntf / (t_b / 1e3), 1),
+            "sequential_ms": round(t_s, 2),
+            "batched_over_sequential": round(t_s / t_b, 3),
+            "setup_s": round(setup_s, 1), "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_storage(args):
+    """c3: one shot of Born forward + RTM adjoint per level storage (FP32,
+    BF16, FP16 with per-level power-of-two scales), each timed with CUDA
+    events on the handle's stream; the 16-bit results are compared with the
+    FP32 result of the same run (the FP64 comparison needs the CPU oracle and
+    is made at test sizes)."""
+    import torch
+    born = package()
+    born.lib()
+    wl = workload_module()
+    t0 = time.perf_counter()
+    case = wl.prepare_shot(born, args.config, nt=args.nt, n=args.model_n)
+    setup_s = time.perf_counter() - t0
+    nz, ny, nx = case["shape"]
+    nt, jt = case["nt"], case["jts"]
+    n_int = wl.interior_cells(case["shape"])
+    # compulsory bytes per interior cell of the three loops (fields 4 or 2 B)
+    bpc = {"f32": (32, 16, 40), "bf16": (20, 10, 28), "f16": (20, 10, 28)}
+    res, ref = {}, None
+    for st in args.storage.split(","):
+        prop = born.Gb300Prop(0)
+        prop.createSpace(case["d"], case["d"], case["d"], 50.0, 0.0005,
+                         0.0005, nx, ny, nz)
+        prop.transferSincTableS(8, jt, case["table_s"])
+        prop.transferSincTableD(8, jt, case["table_d"])
+        prop.transferSourceFunc(9, case["nt_big"], case["locs_s"],
+                                case["src"])
+        prop.transferVelFunc1(nx, ny, nz, case["vel1"])
+        prop.transferVelFunc2(nx, ny, nz, case["vel2"])
+        rec = np.ascontiguousarray(case["rec_in"])
+        prop.transferReceiverFunc(case["rec_nx"], case["rec_ny"],
+                                  case["nt_big"], case["locs_r"], rec)
+        prop.check(prop.lib.born_set_reflectivity(prop.h,
+                                                  born.fptr(case["refl"])))
+        prop.set_storage(st)
+        stream = torch.cuda.ExternalStream(prop.stream, device=0)
+
+        def step(n_steps, ev=None):
+            prop.zero_traces()
+            if ev:
+                ev[0].record(stream)
+            prop.rtm_forward_device(jt, n_steps)
+            if ev:
+                ev[1].record(stream)
+            prop.source_prop_device(jt, n_steps)
+            if ev:
+                ev[2].record(stream)
+            prop.rtm_adjoint_device(jt, n_steps, swap=1)
+            if ev:
+                ev[3].record(stream)
+
+        for _ in range(args.warmup):  # short loops: tuning and first touch
+            step(8)
+        prop.synchronize()
+        ms = [0.0, 0.0, 0.0]
+        with Clocks(0) as clk:
+            for _ in range(args.steps):
+                ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+                step(nt, ev)
+                prop.synchronize()
+                for k in range(3):
+                    ms[k] += ev[k].elapsed_time(ev[k + 1]) / args.steps
+        # the timed run leaves the image of the adjoint; the traces of the
+        # forward loop were overwritten by nothing since
+        img = prop.get_image()
+        tr = prop.get_traces(rec)
+        fwd, src, adj = ms
+        b = bpc[st]
+        r = {"ms": round(fwd + src + adj, 1),
+             "value": round(2 * n_int * nt / ((fwd + src + adj) / 1e3) / 1e9,
+                            3),
+             "forward_ms": round(fwd, 1), "source_ms": round(src, 1),
+             "adjoint_ms": round(adj, 1),
+             "adjoint_GBps": round(b[2] * n_int * nt / (adj / 1e3) / 1e9, 1),
+             "forward_GBps": round(b[0] * n_int * nt / (fwd / 1e3) / 1e9, 1),
+             "clocks": clk.summary()}
+        if ref is None:
+            ref = (img, tr, r["ms"], st)
+        else:
+            def rel(a, b_):
+                return float(np.linalg.norm((a - b_).ravel()) /
+                             max(np.linalg.norm(b_.ravel()), 1e-30))
+            r[f"image_rel_l2_vs_{ref[3]}"] = rel(img, ref[0])
+            r[f"traces_rel_l2_vs_{ref[3]}"] = rel(tr, ref[1])
+            r[f"speedup_vs_{ref[3]}"] = round(ref[2] / r["ms"], 3)
+        res[st] = r
+        del prop
+        torch.cuda.synchronize()
+    first = res[args.storage.split(",")[0]]
+    line = {"metric": "Gcell-updates/s Born fwd+adj per storage (c3)",
+            "value": first["value"], "unit": "Gcell-updates/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": first["ms"], "higher_is_better": True,
+            "dtype": "f32 arithmetic; levels " + args.storage,
+            "data": "synthetic (seeded, shapes of the config)",
+            "config": {"workload": f"{args.config}: Born forward + RTM adjoint,"
+                       f" compute grid {nx}x{ny}x{nz}, nt={nt}, jt={jt}",
+                       "grid": [nz, ny, nx], "nt": nt, "jt": jt,
+                       "interior_cells": n_int},
+            "storage": res, "setup_s": round(setup_s, 1)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", default="c2", choices=["c1", "c2"])
+    ap.add_argument("--config", default="c2",
+                    choices=["c1", "c2", "c3", "c4"])
+    ap.add_argument("--storage", default=None,
+                    help="level storage: f32, bf16 or f16 (c3: a comma list,"
+                         " default f32,bf16,f16; c4: one, default f32)")
+    ap.add_argument("--shots", type=int, default=48,
+                    help="c4: number of shots in the batch")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="c4: launch step by step instead of CUDA graphs")
     ap.add_argument("--model-n", type=int, default=None,
                     help="smaller model edge (profiling cases)")
     ap.add_argument("--nt", type=int, default=None,
@@ -476,6 +661,12 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.config == "c3":
+        args.storage = args.storage or "f32,bf16,f16"
+        return run_storage(args)
+    if args.config == "c4":
+        args.storage = args.storage or "f32"
+        return run_batched(args)
     return run_gpu_arm(args)
 
 

@@ -236,6 +236,38 @@ int born_dot_f64(born_op *op, const float *a, const float *b, long long n,
 int born_cg_solve(born_op *op, const float *data, float *model, int niter,
                   double *resid);
 
+/* ======================================================================
+ * 4. Batched shots
+ *
+ * A batch advances several fully set-up shot handles together: every time
+ * step is one launch covering all shots' tiles (shots may have different
+ * grids), and with graphs on (default) each whole time loop is recorded once
+ * into a CUDA graph and replayed.  All shots must share the sinc tables,
+ * trace lengths and grid spacing.  Results stay in each shot handle (read
+ * them with born_get_image / born_get_traces; work later queued on a shot's
+ * stream waits for the batch).  A shot handle must not run its own time
+ * loops while a batch that holds it is running.  Reallocating a shot's
+ * buffers (create_space, new point sets, new sinc tables) makes the batch
+ * rebuild its descriptors and graphs on the next call.
+ * ====================================================================== */
+typedef struct born_batch born_batch;
+int born_batch_create(born_handle *const *shots, int nshots,
+                      born_batch **out);
+int born_batch_destroy(born_batch *b);
+const char *born_batch_error(const born_batch *b);
+int born_batch_set_graph(born_batch *b, int use_graph);
+void *born_batch_stream(born_batch *b);
+/* Kernels the batch has run (a replayed time loop counts its kernels) and
+ * replays of recorded time loops. */
+long long born_batch_launches(const born_batch *b);
+long long born_batch_graph_launches(const born_batch *b);
+/* born_source_prop / born_rtm_adjoint (swap = 1) / born_rtm_forward for
+ * every shot of the batch, with device-resident results. */
+int born_batch_source_prop(born_batch *b, int jts, int nt);
+int born_batch_rtm_adjoint(born_batch *b, int jtd, int nt);
+int born_batch_rtm_forward(born_batch *b, int jt, int nt);
+int born_batch_synchronize(born_batch *b);
+
 /* FP64 dot product that allocates nothing.  No counterpart in the
  * reference.  For callers that cannot allocate device memory where they need
  * a dot product: applications whose GPU memory is all owned by their own
@@ -269,6 +301,25 @@ int born_tuned_config(const born_handle *h, int mode, int *cfg,
                       float *ms_per_launch);
 /* Kernels launched on this handle since creation (for accounting). */
 long long born_kernel_launches(const born_handle *h);
+
+/* Storage of the propagated wavefield levels.  No counterpart in the
+ * reference (its levels are float).  BF16 and FP16 store every level as
+ * 16-bit values with a power-of-two scale of its own (chosen on the device
+ * from a bound on the level's magnitude, so FP16 neither overflows nor
+ * underflows), while the stencil, the taper, injection, extraction, the Born
+ * coupling and the image stay FP32; velocities, reflectivity, image and
+ * traces stay FP32.  16-bit storage halves the bytes of every level read and
+ * write; its error against an FP64 propagation is that of rounding every
+ * stored level (it grows with the number of steps).  Supported by the
+ * source, rtm adjoint and rtm forward loops (handle and batch); modelling,
+ * the exact linearised pair, host copies of the source levels and the
+ * operator need FP32 and return BORN_ESTATE otherwise.  Needs nx % 8 == 0.
+ * Changing it clears the levels (run source_prop again). */
+#define BORN_STORE_F32 0
+#define BORN_STORE_BF16 1
+#define BORN_STORE_F16 2
+int born_set_storage(born_handle *h, int storage);
+int born_get_storage(const born_handle *h);
 /* Raw CUDA stream of the handle (cudaStream_t), for event timing. */
 void *born_stream(born_handle *h);
 

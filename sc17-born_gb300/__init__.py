@@ -86,10 +86,25 @@ _SIGS = {
     "born_synchronize": (C.c_int, [_vp]),
     "born_tile_config_count": (C.c_int, []),
     "born_set_tiling": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "born_set_storage": (C.c_int, [_vp, C.c_int]),
+    "born_get_storage": (C.c_int, [_vp]),
     "born_autotune": (C.c_int, [_vp, C.c_int]),
     "born_tuned_config": (C.c_int, [_vp, C.c_int, _ip, _fp]),
     "born_kernel_launches": (C.c_longlong, [_vp]),
     "born_stream": (_vp, [_vp]),
+    # batched shots (include/born_gb300.h section 4)
+    "born_batch_create": (C.c_int, [C.POINTER(_vp), C.c_int,
+                                    C.POINTER(_vp)]),
+    "born_batch_destroy": (C.c_int, [_vp]),
+    "born_batch_error": (C.c_char_p, [_vp]),
+    "born_batch_set_graph": (C.c_int, [_vp, C.c_int]),
+    "born_batch_stream": (_vp, [_vp]),
+    "born_batch_launches": (C.c_longlong, [_vp]),
+    "born_batch_graph_launches": (C.c_longlong, [_vp]),
+    "born_batch_source_prop": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "born_batch_rtm_adjoint": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "born_batch_rtm_forward": (C.c_int, [_vp, C.c_int, C.c_int]),
+    "born_batch_synchronize": (C.c_int, [_vp]),
     # operator and CG (include/born_gb300.h section 3)
     "born_op_create": (C.c_int, [_vp, _vp, _fp, _fp, _fp, C.POINTER(_vp)]),
     "born_op_destroy": (C.c_int, [_vp]),
@@ -229,6 +244,18 @@ class Handle:
 
     def autotune(self, enable: bool = True):
         self.check(self.lib.born_autotune(self.h, int(enable)))
+
+    STORAGE = {"f32": 0, "bf16": 1, "f16": 2}
+
+    def set_storage(self, storage: str = "f32"):
+        """Storage of the wavefield levels: "f32", "bf16" or "f16" (16-bit
+        values with a power-of-two scale per level, FP32 arithmetic)."""
+        self.check(self.lib.born_set_storage(self.h, self.STORAGE[storage]))
+
+    @property
+    def storage(self) -> str:
+        k = int(self.lib.born_get_storage(self.h))
+        return {v: n for n, v in self.STORAGE.items()}[k]
 
     def tuned_config(self, mode: int):
         cfg, ms = C.c_int(), C.c_float()
@@ -391,6 +418,66 @@ class Gb300Prop(Handle):
 
     def zero_traces(self):
         self.check(self.lib.born_zero_traces(self.h))
+
+
+# ---------------------------------------------------------------------------
+# Batched shots
+
+class Batch:
+    """Several set-up shots (Gb300Prop) advanced together: one launch per
+    time step for all shots, each time loop recorded once into a CUDA graph
+    (``graph=False`` launches step by step).  Results stay in the shots."""
+
+    def __init__(self, shots, graph: bool = True):
+        self.lib = lib()
+        self.shots = list(shots)  # keeps the handles alive
+        arr = (_vp * len(self.shots))(*[s.h for s in self.shots])
+        b = _vp()
+        rc = self.lib.born_batch_create(arr, len(self.shots), C.byref(b))
+        if rc != BORN_OK:
+            raise BornError(rc, "born_batch_create failed")
+        self.b = b
+        self.check(self.lib.born_batch_set_graph(b, int(graph)))
+
+    def check(self, rc):
+        if rc != BORN_OK:
+            msg = self.lib.born_batch_error(self.b)
+            raise BornError(rc, msg.decode() if msg else "")
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.born_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.born_batch_stream(self.b) or 0)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.born_batch_launches(self.b))
+
+    @property
+    def graph_launches(self) -> int:
+        return int(self.lib.born_batch_graph_launches(self.b))
+
+    def source_prop(self, jts, nt):
+        self.check(self.lib.born_batch_source_prop(self.b, jts, nt))
+
+    def rtm_adjoint(self, jtd, nt):
+        self.check(self.lib.born_batch_rtm_adjoint(self.b, jtd, nt))
+
+    def rtm_forward(self, jt, nt):
+        self.check(self.lib.born_batch_rtm_forward(self.b, jt, nt))
+
+    def synchronize(self):
+        self.check(self.lib.born_batch_synchronize(self.b))
 
 
 # ---------------------------------------------------------------------------

@@ -132,6 +132,19 @@ int upload_points(born_handle *h, DevPoints &dp, int npts, int nt,
       return fail(h, BORN_EINVAL,
                   "point %d at cell %d is outside the interior [4, n-4)", i,
                   locs[i]);
+  const size_t tbytes = (size_t)npts * nt * sizeof(float);
+  if (dp.plane_off && dp.npts == npts && dp.nt == nt &&
+      std::equal(dp.host_locs.begin(), dp.host_locs.end(), locs)) {
+    // same points and trace length (the next shot's data over the same
+    // geometry): only the trace values change, so the buffers, descriptors
+    // and recorded graphs that use them stay valid
+    int rc = set_device(h);
+    if (rc) return rc;
+    if (tbytes)
+      CK(h, cudaMemcpyAsync(dp.traces, traces, tbytes, cudaMemcpyHostToDevice,
+                            h->stream));
+    return BORN_OK;
+  }
   std::vector<int> order(npts);
   for (int i = 0; i < npts; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(),
@@ -151,6 +164,11 @@ int upload_points(born_handle *h, DevPoints &dp, int npts, int nt,
   if ((long long)planes.size() * n12 >= (1ll << 31))
     return fail(h, BORN_EINVAL, "points span too many planes");
   std::vector<int> head(std::max<size_t>(1, planes.size() * n12), -1);
+  int mult = 1;
+  for (int s = 1, run = 1; s < npts; ++s) {
+    run = slot_cell[s] == slot_cell[s - 1] ? run + 1 : 1;
+    mult = std::max(mult, run);
+  }
   for (int s = npts - 1; s >= 0; --s) {
     const int z = (int)(slot_cell[s] / n12);
     head[plane_off[z] + (slot_cell[s] % n12)] = s;
@@ -158,10 +176,12 @@ int upload_points(born_handle *h, DevPoints &dp, int npts, int nt,
   int rc = set_device(h);
   if (rc) return rc;
   cudaStreamSynchronize(h->stream);
-  const size_t tbytes = (size_t)npts * nt * sizeof(float);
   DevPoints nd;
   nd.npts = npts;
   nd.nt = nt;
+  nd.host_locs.assign(locs, locs + npts);
+  nd.mult = mult;
+  nd.absmax = h->stat_dev + (&dp == &h->src ? kStatSrc : kStatRec);
   for (int z : planes) {
     nd.zlo = std::min(nd.zlo, z);
     nd.zhi = std::max(nd.zhi, z);
@@ -185,12 +205,16 @@ int upload_points(born_handle *h, DevPoints &dp, int npts, int nt,
   }
   dp.release();
   dp = nd;
+  h->generation++;
   return BORN_OK;
 }
 
-int get_map(born_handle *h, const float *buf, int cfg, int kind,
+// TMA descriptor of a grid buffer: kind 0 = halo box (TX+8) x (TY+8),
+// kind 1 = centre tile (TX x TY for FP32, (TX+8) x TY for 16-bit elements,
+// whose copies must start at x multiples of 8).
+int get_map(born_handle *h, const void *buf, int cfg, int kind, int esize,
             CUtensorMap *out) {
-  auto key = std::make_pair((const void *)buf, cfg * 2 + kind);
+  auto key = std::make_pair(buf, (cfg * 2 + kind) * 8 + esize);
   auto it = h->maps.find(key);
   if (it != h->maps.end()) {
     *out = it->second;
@@ -203,13 +227,17 @@ int get_map(born_handle *h, const float *buf, int cfg, int kind,
   CUtensorMap m;
   const cuuint64_t dims[3] = {(cuuint64_t)h->n1, (cuuint64_t)h->n2,
                               (cuuint64_t)h->n3};
-  const cuuint64_t strides[2] = {(cuuint64_t)h->n1 * 4,
-                                 (cuuint64_t)h->n1 * h->n2 * 4};
+  const cuuint64_t strides[2] = {(cuuint64_t)h->n1 * esize,
+                                 (cuuint64_t)h->n1 * h->n2 * esize};
   const int halo = kind == 0 ? 2 * born::kRadius : 0;
-  const cuuint32_t box[3] = {(cuuint32_t)(tx + halo), (cuuint32_t)(ty + halo),
+  const int xhalo = (kind == 0 || esize == 2) ? 2 * born::kRadius : 0;
+  const cuuint32_t box[3] = {(cuuint32_t)(tx + xhalo), (cuuint32_t)(ty + halo),
                              1};
   const cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)buf, dims,
+  CUresult r = enc(&m,
+                   esize == 2 ? CU_TENSOR_MAP_DATA_TYPE_UINT16
+                              : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                   3, (void *)buf, dims,
                    strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -225,7 +253,7 @@ int get_map(born_handle *h, const float *buf, int cfg, int kind,
 void pick_tiling(born_handle *h, int mode, bool pa, bool pb, int *cfg,
                  int *zseg, int *tiles_x, int *tiles_y) {
   int c = h->tile_cfg >= 0                ? h->tile_cfg
-          : h->tuned_cfg[mode] >= 0 ? h->tuned_cfg[mode]
+          : h->tuned_cfg[h->storage][mode] >= 0 ? h->tuned_cfg[h->storage][mode]
                                           : 0;
   int tx, ty;
   born::tile_cfg_dims(c, &tx, &ty);
@@ -239,7 +267,7 @@ void pick_tiling(born_handle *h, int mode, bool pa, bool pb, int *cfg,
   }
   int sms = 148;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-  const size_t smem = born::step_smem_bytes(c, mode, pa, pb);
+  const size_t smem = born::step_smem_bytes(h->storage, c, mode, pa, pb);
   int per_sm = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
   per_sm = std::min(per_sm, 2048 / ((tx / 4) * ty));
   const long long target = 2ll * sms * per_sm;
@@ -264,6 +292,8 @@ PointSet point_view(const DevPoints &dp, int id, int ii,
   ps.zhi = dp.zhi;
   ps.id = id;
   ps.scale = scale;
+  ps.absmax = dp.absmax;
+  ps.mult = dp.mult;
   ps.active = use && dp.npts > 0 && (id + 7 < dp.nt) ? 1 : 0;
   if (ps.active)
     for (int k = 0; k < 8; ++k) ps.tab[k] = tab[(size_t)ii * 8 + k];
@@ -278,12 +308,20 @@ void base_params(born_handle *h, StepParams &p) {
   memcpy(p.c, h->coeffs, sizeof(p.c));
   memcpy(p.bound, h->bound, sizeof(p.bound));
   p.err = h->err_dev;
+  p.lv = h->lv_dev;
+  float cs = std::fabs(h->coeffs[0]);
+  for (int i = 1; i < 13; ++i) cs += 2.f * std::fabs(h->coeffs[i]);
+  p.csum = cs;
+  p.la = p.lb = born::LevelRefs{-1, -1, -1, 0u};
+  p.vmax_a = p.vmax_b = p.imgmax = h->stat_dev;  // set per mode when used
 }
 
 // One step launch.  a_cur / b_cur: current levels of the propagated fields
-// (halo boxes); centre[slot]: the per-cell inputs by born::CentreSlot.
-int launch(born_handle *h, int mode, bool pa, bool pb, const float *a_cur,
-           const float *b_cur, const float *const centre[born::kNumCentre],
+// (halo boxes); centre[slot]: the per-cell inputs by born::CentreSlot.  With
+// 16-bit storage the field levels (a_cur, b_cur and the previous-level
+// slots) are 16-bit buffers.
+int launch(born_handle *h, int mode, bool pa, bool pb, const void *a_cur,
+           const void *b_cur, const void *const centre[born::kNumCentre],
            StepParams &p) {
   int cfg, zseg, tx, ty;
   pick_tiling(h, mode, pa, pb, &cfg, &zseg, &tx, &ty);
@@ -291,20 +329,26 @@ int launch(born_handle *h, int mode, bool pa, bool pb, const float *a_cur,
   p.tiles_y = ty;
   p.zseg = zseg;
   born::StepMaps maps;
+  const int fe = h->level_esize();
   const float *any = h->vel2;  // any valid grid buffer for unused slots
-  int rc = get_map(h, a_cur ? a_cur : any, cfg, 0, &maps.box_a);
-  if (!rc) rc = get_map(h, b_cur ? b_cur : any, cfg, 0, &maps.box_b);
-  if (!rc) rc = get_map(h, a_cur ? a_cur : any, cfg, 1, &maps.zc_a);
-  if (!rc) rc = get_map(h, b_cur ? b_cur : any, cfg, 1, &maps.zc_b);
+  // unused field maps still need a valid descriptor: any buffer of the
+  // field's element size (a level buffer with 16-bit storage)
+  const void *anyf = fe == 4 ? (const void *)any : (const void *)h->f0;
+  int rc = get_map(h, a_cur ? a_cur : anyf, cfg, 0, fe, &maps.box_a);
+  if (!rc) rc = get_map(h, b_cur ? b_cur : anyf, cfg, 0, fe, &maps.box_b);
+  if (!rc) rc = get_map(h, a_cur ? a_cur : anyf, cfg, 1, fe, &maps.zc_a);
+  if (!rc) rc = get_map(h, b_cur ? b_cur : anyf, cfg, 1, fe, &maps.zc_b);
   const unsigned mask = born::centre_mask(mode, pa, pb);
   for (int sl = 0; sl < born::kNumCentre && !rc; ++sl) {
     const bool used = mask & (1u << sl);
     if (used && !centre[sl])
       return fail(h, BORN_ESTATE, "step input %d missing", sl);
-    rc = get_map(h, used ? centre[sl] : any, cfg, 1, &maps.cm[sl]);
+    const int es = born::field_slot(mode, sl) ? fe : 4;
+    rc = get_map(h, used ? centre[sl] : (es == 4 ? (const void *)any : anyf),
+                 cfg, 1, es, &maps.cm[sl]);
   }
   if (rc) return rc;
-  CK(h, born::launch_step(mode, pa, pb, cfg, maps, p, h->stream));
+  CK(h, born::launch_step(h->storage, mode, pa, pb, cfg, maps, p, h->stream));
   h->launches++;
   return BORN_OK;
 }
@@ -313,13 +357,17 @@ int check_device_error(born_handle *h);
 
 // Autotuner: times every tile configuration of one step mode on the
 // current grid (one warm-up and three timed launches, CUDA events on the
-// handle's stream) and keeps the fastest.  It runs on the scratch levels
-// f0/f1/r0/r1 and the image with every point set inactive, so it never
-// touches the source levels kept for rtm_adjoint, and clears what it used.
+// handle's stream) and keeps the fastest, per storage type.  It runs on the
+// scratch levels f0/f1/r0/r1 and a temporary image with every point set
+// inactive, so it never touches the source levels kept for rtm_adjoint nor
+// an image a caller has yet to read, and clears the levels it used.
 int tune_mode(born_handle *h, int mode) {
   const bool pb = mode == kModeForward || mode == kModeAdjoint ||
                   mode == born::kModeBornLin;
   if (!h->have_vel1 || !h->have_vel2) return BORN_OK;  // nothing to time yet
+  float *timg = nullptr;
+  CK(h, cudaMalloc(&timg, (size_t)h->n123 * 4));
+  CK(h, cudaMemsetAsync(timg, 0, (size_t)h->n123 * 4, h->stream));
   cudaEvent_t e0, e1;
   CK(h, cudaEventCreate(&e0));
   CK(h, cudaEventCreate(&e1));
@@ -327,15 +375,26 @@ int tune_mode(born_handle *h, int mode) {
   int best = -1;
   float best_ms = 0.f;
   int rc = BORN_OK;
+  const bool lp = h->storage != born::kStoreF32;
+  if (lp) {
+    const void *reset[] = {h->f0, h->f1, h->r0, h->r1};
+    rc = born_lp_prologue(h, h->stream, reset, 4);
+  }
   for (int cfg = 0; cfg < born::tile_cfg_count() && !rc; ++cfg) {
     h->tile_cfg = cfg;
     StepParams p;
     base_params(h, p);
     p.a_out = h->f1;
     p.b_out = h->r1;
-    p.img_out = h->img;
-    const float *cen[born::kNumCentre] = {h->f1, h->r1, h->vel2, h->vel1,
-                                          h->img};
+    p.img_out = timg;
+    if (lp) {
+      born_set_lp_words(h, p, mode);
+      // fixed record slots: the levels stay zero with every point inactive
+      p.la = born_level_refs(h, h->f0, h->f1, true, 1u);
+      p.lb = born_level_refs(h, h->r0, h->r1, true, 1u);
+    }
+    const void *cen[born::kNumCentre] = {h->f1, h->r1, h->vel2, h->vel1,
+                                         mode == kModeForward ? h->refl : timg};
     for (int it = 0; it < 4 && !rc; ++it) {
       if (it == 1) cudaEventRecord(e0, h->stream);
       rc = launch(h, mode, true, pb, h->f0, h->r0, cen, p);
@@ -352,17 +411,19 @@ int tune_mode(born_handle *h, int mode) {
   h->tile_cfg = saved;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  cudaStreamSynchronize(h->stream);
+  cudaFree(timg);
   if (rc) return rc;
-  h->tuned_cfg[mode] = best;
-  h->tuned_ms[mode] = best_ms / 3.f;
-  const size_t bytes = (size_t)h->n123 * 4;
-  float *scratch[] = {h->f0, h->f1, h->r0, h->r1, h->img};
+  h->tuned_cfg[h->storage][mode] = best;
+  h->tuned_ms[h->storage][mode] = best_ms / 3.f;
+  const size_t bytes = h->level_bytes();
+  float *scratch[] = {h->f0, h->f1, h->r0, h->r1};
   for (float *b : scratch) CK(h, cudaMemsetAsync(b, 0, bytes, h->stream));
   return check_device_error(h);
 }
 
 int ensure_tuned(born_handle *h, int mode) {
-  if (!h->autotune || h->tile_cfg >= 0 || h->tuned_cfg[mode] >= 0)
+  if (!h->autotune || h->tile_cfg >= 0 || h->tuned_cfg[h->storage][mode] >= 0)
     return BORN_OK;
   return tune_mode(h, mode);
 }
@@ -416,7 +477,101 @@ int born_fail(born_handle *h, int code, const char *fmt, ...) {
   return code;
 }
 int born_check_ready(born_handle *h) { return check_ready(h); }
+born::PointSet born_point_view(const DevPoints &dp, int id, int ii,
+                               const std::vector<float> &tab, float scale,
+                               bool use) {
+  return point_view(dp, id, ii, tab, scale, use);
+}
+void born_base_params(born_handle *h, StepParams &p) { base_params(h, p); }
+int born_get_map(born_handle *h, const void *buf, int cfg, int kind,
+                 int esize, CUtensorMap *out) {
+  return get_map(h, buf, cfg, kind, esize, out);
+}
+void born_pick_tiling(born_handle *h, int mode, bool pa, bool pb, int *cfg,
+                      int *zseg, int *tiles_x, int *tiles_y) {
+  pick_tiling(h, mode, pa, pb, cfg, zseg, tiles_x, tiles_y);
+}
+int born_ensure_tuned(born_handle *h, int mode) { return ensure_tuned(h, mode); }
 int born_check_device_error(born_handle *h) { return check_device_error(h); }
+
+int born_level_id(const born_handle *h, const void *buf) {
+  const void *b[kNumLevelBufs] = {h->s0, h->s1, h->r0, h->r1, h->f0, h->f1};
+  for (int i = 0; i < kNumLevelBufs; ++i)
+    if (buf && b[i] == buf) return i;
+  return -1;
+}
+
+born::LevelRefs born_level_refs(const born_handle *h, const void *cur,
+                                const void *old, bool write, unsigned int tag) {
+  born::LevelRefs r{-1, -1, -1, tag};
+  const int c = born_level_id(h, cur), o = born_level_id(h, old);
+  if (c >= 0) r.cur = 2 * c + (h->wr[c] & 1);
+  if (o >= 0) {
+    r.old = 2 * o + (h->wr[o] & 1);
+    if (write) r.out = 2 * o + ((h->wr[o] + 1) & 1);
+  }
+  return r;
+}
+
+void born_level_written(born_handle *h, const void *buf) {
+  const int i = born_level_id(h, buf);
+  if (i >= 0) h->wr[i]++;
+}
+
+int born_lp_prologue(born_handle *h, cudaStream_t s, const void *const *reset,
+                     int nreset) {
+  if (h->storage == born::kStoreF32) return BORN_OK;
+  unsigned int *st = h->stat_dev;
+  CK(h, cudaMemsetAsync(st, 0, kNumStats * sizeof(unsigned int), s));
+  const float *arr[3] = {h->vel1, h->vel2, h->refl};
+  for (int k = 0; k < 3; ++k) {
+    CK(h, born::launch_absmax(arr[k], h->n123, st + k, s));
+    h->launches++;
+  }
+  const DevPoints *pts[2] = {&h->src, &h->rec};
+  for (int k = 0; k < 2; ++k)
+    if (pts[k]->npts > 0) {
+      CK(h, born::launch_absmax(pts[k]->traces,
+                                (long long)pts[k]->npts * pts[k]->nt,
+                                st + kStatSrc + k, s));
+      h->launches++;
+    }
+  for (int i = 0; i < nreset; ++i) {
+    const int id = born_level_id(h, reset[i]);
+    if (id < 0) continue;
+    CK(h, born::launch_level_reset(h->lv_dev, id, s));
+    h->launches++;
+    h->wr[id] = 0;
+  }
+  return BORN_OK;
+}
+
+int born_copy_level(born_handle *h, void *dst, const void *src,
+                    unsigned int tag, cudaStream_t s) {
+  CK(h, cudaMemcpyAsync(dst, src, h->level_bytes(), cudaMemcpyDeviceToDevice,
+                        s));
+  const int d = born_level_id(h, dst), c = born_level_id(h, src);
+  if (h->storage != born::kStoreF32 && d >= 0 && c >= 0) {
+    CK(h, born::launch_level_copy(h->lv_dev, 2 * d + ((h->wr[d] + 1) & 1),
+                                  2 * c + (h->wr[c] & 1), tag, s));
+    h->launches++;
+  }
+  if (d >= 0) h->wr[d]++;
+  return BORN_OK;
+}
+
+void born_set_lp_words(born_handle *h, StepParams &p, int mode) {
+  unsigned int *st = h->stat_dev;
+  if (mode == kModeSource) {
+    p.vmax_a = p.vmax_b = st + kStatVel1;
+  } else if (mode == kModeAdjoint) {
+    p.vmax_a = st + kStatVel2;  // receiver field through vel2
+    p.vmax_b = st + kStatVel1;  // source field rebuilt through vel1
+  } else {
+    p.vmax_a = p.vmax_b = st + kStatVel2;
+  }
+  p.imgmax = st + kStatRefl;
+}
 
 // ===========================================================================
 // Handle API
@@ -434,8 +589,23 @@ int born_create(int device, born_handle **out) {
       cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) !=
           cudaSuccess ||
       cudaMalloc(&h->err_dev, sizeof(unsigned int)) != cudaSuccess ||
-      cudaMemset(h->err_dev, 0, sizeof(unsigned int)) != cudaSuccess) {
+      cudaMemset(h->err_dev, 0, sizeof(unsigned int)) != cudaSuccess ||
+      cudaMalloc(&h->lv_dev, kNumLevelBufs * 4 * sizeof(unsigned long long)) !=
+          cudaSuccess ||
+      cudaMalloc(&h->stat_dev, kNumStats * sizeof(unsigned int)) !=
+          cudaSuccess ||
+      cudaMemset(h->stat_dev, 0, kNumStats * sizeof(unsigned int)) !=
+          cudaSuccess) {
+    cudaFree(h->err_dev);
+    cudaFree(h->lv_dev);
+    cudaFree(h->stat_dev);
     delete h;
+    return BORN_ECUDA;
+  }
+  for (int b = 0; b < kNumLevelBufs; ++b)
+    born::launch_level_reset(h->lv_dev, b, h->stream);
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) {
+    born_destroy(h);
     return BORN_ECUDA;
   }
   *out = h;
@@ -450,6 +620,8 @@ int born_destroy(born_handle *h) {
   h->src.release();
   h->rec.release();
   cudaFree(h->err_dev);
+  cudaFree(h->lv_dev);
+  cudaFree(h->stat_dev);
   cudaStreamDestroy(h->stream);
   delete h;
   return BORN_OK;
@@ -499,6 +671,7 @@ int born_create_space(born_handle *h, float d1, float d2, float d3, float bc_a,
   }
   CK(h, cudaStreamSynchronize(h->stream));
   h->have_space = true;
+  h->generation++;
   return BORN_OK;
 }
 
@@ -508,6 +681,7 @@ int born_set_sinc_table(born_handle *h, int which, int nsinc, int jt,
   if (nsinc != 8 || jt < 1 || !table || (which != 0 && which != 1))
     return fail(h, BORN_EINVAL, "sinc table: need nsinc == 8, jt >= 1");
   std::vector<float> t(table, table + (size_t)jt * 8);
+  h->generation++;  // table values are baked into recorded graphs
   if (which == 0) {
     h->tab_s = t;
     h->jt_s = jt;
@@ -568,12 +742,19 @@ int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
   if (nt < 0 || jts < 1) return fail(h, BORN_EINVAL, "nt < 0 or jts < 1");
   if (!h->have_vel1) return fail(h, BORN_ESTATE, "vel1 not transferred");
   if (h->jt_s < 1) return fail(h, BORN_ESTATE, "source sinc table missing");
+  if ((p0_out || p1_out) && h->storage != born::kStoreF32)
+    return fail(h, BORN_ESTATE, "host copies of the levels need FP32 storage");
   h->jt = jts;
   rc = ensure_tuned(h, kModeSource);
   if (rc) return rc;
-  const size_t bytes = (size_t)h->n123 * 4;
-  CK(h, cudaMemsetAsync(h->s0, 0, bytes, h->stream));
-  CK(h, cudaMemsetAsync(h->s1, 0, bytes, h->stream));
+  const size_t lbytes = h->level_bytes(), bytes = (size_t)h->n123 * 4;
+  CK(h, cudaMemsetAsync(h->s0, 0, lbytes, h->stream));
+  CK(h, cudaMemsetAsync(h->s1, 0, lbytes, h->stream));
+  {
+    const void *reset[] = {h->s0, h->s1};
+    rc = born_lp_prologue(h, h->stream, reset, 2);
+    if (rc) return rc;
+  }
   float *p0 = h->s0, *p1 = h->s1;
   const float scale = 1 / (float)jts;
   for (int it = 0; it <= nt; ++it) {
@@ -583,15 +764,20 @@ int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
     p.a_out = p0;
     p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
     p.pb = point_view(h->src, 0, 0, h->tab_s, 0.f, false);
-    const float *cen[born::kNumCentre] = {p0, nullptr, h->vel1, nullptr,
-                                          nullptr};
+    born_set_lp_words(h, p, kModeSource);
+    p.la = born_level_refs(h, p1, p0, true, kTagSource + it);
+    const void *cen[born::kNumCentre] = {p0, nullptr, h->vel1, nullptr,
+                                         nullptr};
     rc = launch(h, kModeSource, true, false, p1, nullptr, cen, p);
     if (!rc) rc = poll_error(h, it);
     if (rc) return rc;
+    born_level_written(h, p0);
     std::swap(p0, p1);
   }
-  if (nt % 2 == 1)
-    CK(h, cudaMemcpyAsync(p1, p0, bytes, cudaMemcpyDeviceToDevice, h->stream));
+  if (nt % 2 == 1) {
+    rc = born_copy_level(h, p1, p0, kTagSource + nt + 1, h->stream);
+    if (rc) return rc;
+  }
   h->src_levels_valid = true;
   if (p0_out) CK(h, cudaMemcpyAsync(p0_out, h->s0, bytes, cudaMemcpyDeviceToHost, h->stream));
   if (p1_out) CK(h, cudaMemcpyAsync(p1_out, h->s1, bytes, cudaMemcpyDeviceToHost, h->stream));
@@ -614,9 +800,14 @@ int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap,
     return fail(h, BORN_ESTATE, "no source levels (run source_prop first)");
   rc = ensure_tuned(h, kModeAdjoint);
   if (rc) return rc;
-  const size_t bytes = (size_t)h->n123 * 4;
-  CK(h, cudaMemsetAsync(h->r0, 0, bytes, h->stream));
-  CK(h, cudaMemsetAsync(h->r1, 0, bytes, h->stream));
+  const size_t lbytes = h->level_bytes(), bytes = (size_t)h->n123 * 4;
+  CK(h, cudaMemsetAsync(h->r0, 0, lbytes, h->stream));
+  CK(h, cudaMemsetAsync(h->r1, 0, lbytes, h->stream));
+  {
+    const void *reset[] = {h->r0, h->r1};
+    rc = born_lp_prologue(h, h->stream, reset, 2);
+    if (rc) return rc;
+  }
   // cpuProp accumulates into the caller's image (cpu_prop.cc:101)
   if (img_out)
     CK(h, cudaMemcpyAsync(h->img, img_out, bytes, cudaMemcpyHostToDevice,
@@ -638,11 +829,17 @@ int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap,
     p.img_out = h->img;
     p.pa = point_view(h->rec, id, ii, h->tab_d, scale, true);
     p.pb = pending;
-    const float *cen[born::kNumCentre] = {rp0, sp0, h->vel2, h->vel1, h->img};
+    born_set_lp_words(h, p, kModeAdjoint);
+    const unsigned int tag = kTagAdjoint + 2u * (unsigned int)(nt - 1 - it);
+    p.la = born_level_refs(h, pa ? rp1 : nullptr, rp0, true, tag);
+    p.lb = born_level_refs(h, pb ? sp1 : nullptr, sp0, pb, tag + 1u);
+    const void *cen[born::kNumCentre] = {rp0, sp0, h->vel2, h->vel1, h->img};
     rc = launch(h, kModeAdjoint, pa, pb, pa ? rp1 : nullptr,
                 pb ? sp1 : nullptr, cen, p);
     if (!rc) rc = poll_error(h, nt - 1 - it);
     if (rc) return rc;
+    born_level_written(h, rp0);
+    if (pb) born_level_written(h, sp0);
     // the source injection of this step goes into the current level, which
     // the next step reads as its previous level (cpu_prop.cc:79-82)
     pending = point_view(h->src, id_s, i_s, h->tab_s, scale, pb);
@@ -650,7 +847,10 @@ int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap,
     std::swap(rp0, rp1);
   }
   if (pending.active) {
-    CK(h, born::launch_point_inject(pending, h->src.npts, sp0, h->stream));
+    const int id = born_level_id(h, sp0);
+    CK(h, born::launch_point_inject(pending, h->src.npts, sp0, h->storage,
+                                    h->lv_dev, 2 * id + (h->wr[id] & 1),
+                                    h->stream));
     h->launches++;
   }
   if (img_out) {
@@ -673,11 +873,16 @@ int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out) {
   h->jt = jt;
   rc = ensure_tuned(h, kModeForward);
   if (rc) return rc;
-  const size_t bytes = (size_t)h->n123 * 4;
-  CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
-  CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
-  CK(h, cudaMemsetAsync(h->r0, 0, bytes, h->stream));
-  CK(h, cudaMemsetAsync(h->r1, 0, bytes, h->stream));
+  const size_t lbytes = h->level_bytes();
+  CK(h, cudaMemsetAsync(h->f0, 0, lbytes, h->stream));
+  CK(h, cudaMemsetAsync(h->f1, 0, lbytes, h->stream));
+  CK(h, cudaMemsetAsync(h->r0, 0, lbytes, h->stream));
+  CK(h, cudaMemsetAsync(h->r1, 0, lbytes, h->stream));
+  {
+    const void *reset[] = {h->f0, h->f1, h->r0, h->r1};
+    rc = born_lp_prologue(h, h->stream, reset, 4);
+    if (rc) return rc;
+  }
   float *sp0 = h->f0, *sp1 = h->f1, *rp0 = h->r0, *rp1 = h->r1;
   const float scale = 1 / (float)jt;
   for (int it = 0; it < nt; ++it) {
@@ -688,11 +893,17 @@ int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out) {
     p.b_out = rp0;
     p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
     p.pb = point_view(h->rec, id, ii, h->tab_d, 0.f, true);
-    const float *cen[born::kNumCentre] = {sp0, rp0, h->vel2, nullptr,
-                                          h->refl};
+    born_set_lp_words(h, p, kModeForward);
+    const unsigned int tag = kTagForward + 2u * (unsigned int)it;
+    p.la = born_level_refs(h, sp1, sp0, true, tag);
+    p.lb = born_level_refs(h, rp1, rp0, true, tag + 1u);
+    const void *cen[born::kNumCentre] = {sp0, rp0, h->vel2, nullptr,
+                                         h->refl};
     rc = launch(h, kModeForward, true, true, sp1, rp1, cen, p);
     if (!rc) rc = poll_error(h, it);
     if (rc) return rc;
+    born_level_written(h, sp0);
+    born_level_written(h, rp0);
     std::swap(sp0, sp1);
     std::swap(rp0, rp1);
   }
@@ -724,6 +935,8 @@ int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out) {
 int born_model(born_handle *h, int jt, int nt, float *traces_out) {
   int rc = check_ready(h);
   if (rc) return rc;
+  if (h->storage != born::kStoreF32)
+    return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
   if (nt < 0 || jt < 1) return fail(h, BORN_EINVAL, "nt < 0 or jt < 1");
   if (!h->have_vel2) return fail(h, BORN_ESTATE, "vel2 not transferred");
   if (jt > h->jt_s || jt > h->jt_d)
@@ -742,7 +955,7 @@ int born_model(born_handle *h, int jt, int nt, float *traces_out) {
     p.a_out = sp0;
     p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
     p.pb = point_view(h->rec, id, ii, h->tab_d, 0.f, true);
-    const float *cen[born::kNumCentre] = {sp0, nullptr, h->vel2, nullptr,
+    const void *cen[born::kNumCentre] = {sp0, nullptr, h->vel2, nullptr,
                                           nullptr};
     rc = launch(h, born::kModeModel, true, false, sp1, nullptr, cen, p);
     if (!rc) rc = poll_error(h, it);
@@ -761,6 +974,8 @@ int born_model(born_handle *h, int jt, int nt, float *traces_out) {
 int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
   int rc = check_ready(h);
   if (rc) return rc;
+  if (h->storage != born::kStoreF32)
+    return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
   if (nt < 0 || jt < 1) return fail(h, BORN_EINVAL, "nt < 0 or jt < 1");
   if (!h->have_vel2 || !h->have_refl)
     return fail(h, BORN_ESTATE, "vel2 or model perturbation not transferred");
@@ -783,7 +998,7 @@ int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
     p.b_out = rp0;
     p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
     p.pb = point_view(h->rec, id, ii, h->tab_d, 0.f, true);
-    const float *cen[born::kNumCentre] = {sp0, rp0, h->vel2, nullptr,
+    const void *cen[born::kNumCentre] = {sp0, rp0, h->vel2, nullptr,
                                           h->refl};
     rc = launch(h, born::kModeBornLin, true, true, sp1, rp1, cen, p);
     if (!rc) rc = poll_error(h, it);
@@ -816,6 +1031,8 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
                      float *model_out) {
   int rc = check_ready(h);
   if (rc) return rc;
+  if (h->storage != born::kStoreF32)
+    return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
   if (nt < 1 || jt < 1 || interval < 1)
     return fail(h, BORN_EINVAL, "nt, jt and interval must be >= 1");
   if (!h->have_vel2) return fail(h, BORN_ESTATE, "vel2 not transferred");
@@ -838,7 +1055,7 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
     p.g_out = g;
     p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
     p.pb = point_view(h->rec, id, ii, h->tab_d, 0.f, false);
-    const float *cen[born::kNumCentre] = {sp0, nullptr, h->vel2, nullptr,
+    const void *cen[born::kNumCentre] = {sp0, nullptr, h->vel2, nullptr,
                                           nullptr};
     return launch(h, born::kModeModel, true, false, sp1, nullptr, cen, p);
   };
@@ -885,7 +1102,7 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
       p.img_out = h->img;
       p.pa = point_view(h->rec, id, ii, h->tab_d, 1.f, true);
       const float *g = h->gbuf + (size_t)(it - t0) * n;
-      const float *cen[born::kNumCentre] = {wp0, g, h->vel2, nullptr, h->img};
+      const void *cen[born::kNumCentre] = {wp0, g, h->vel2, nullptr, h->img};
       rc = launch(h, born::kModeBornAdj, true, false, wp1, nullptr, cen, p);
       if (!rc) rc = poll_error(h, steps++);
       if (rc) return rc;
@@ -925,6 +1142,8 @@ int born_get_traces(born_handle *h, float *out) {
 int born_get_source_levels(born_handle *h, float *p0_out, float *p1_out) {
   int rc = check_ready(h);
   if (rc) return rc;
+  if (h->storage != born::kStoreF32)
+    return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
   const size_t bytes = (size_t)h->n123 * 4;
   if (p0_out) CK(h, cudaMemcpyAsync(p0_out, h->s0, bytes, cudaMemcpyDeviceToHost, h->stream));
   if (p1_out) CK(h, cudaMemcpyAsync(p1_out, h->s1, bytes, cudaMemcpyDeviceToHost, h->stream));
@@ -934,6 +1153,8 @@ int born_get_source_levels(born_handle *h, float *p0_out, float *p1_out) {
 int born_set_source_levels(born_handle *h, const float *p0, const float *p1) {
   int rc = check_ready(h);
   if (rc) return rc;
+  if (h->storage != born::kStoreF32)
+    return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
   if (!p0 || !p1) return fail(h, BORN_EINVAL, "null source level");
   const size_t bytes = (size_t)h->n123 * 4;
   CK(h, cudaMemcpyAsync(h->s0, p0, bytes, cudaMemcpyHostToDevice, h->stream));
@@ -965,12 +1186,14 @@ int born_autotune(born_handle *h, int enable) {
   int rc = check_ready(h);
   if (rc) return rc;
   h->autotune = enable != 0;
-  for (int m = 0; m < 6; ++m) h->tuned_cfg[m] = -1;
+  for (int st = 0; st < 3; ++st)
+    for (int m = 0; m < 6; ++m) h->tuned_cfg[st][m] = -1;
   if (!enable) return BORN_OK;
   const int modes[] = {kModeSource, kModeForward, kModeAdjoint,
                        born::kModeModel, born::kModeBornLin,
                        born::kModeBornAdj};
   for (int m : modes) {
+    if (h->storage != born::kStoreF32 && m > kModeAdjoint) continue;
     rc = tune_mode(h, m);
     if (rc) return rc;
   }
@@ -980,8 +1203,9 @@ int born_autotune(born_handle *h, int enable) {
 int born_tuned_config(const born_handle *h, int mode, int *cfg,
                       float *ms_per_launch) {
   if (!h || mode < 0 || mode > 5) return BORN_EINVAL;
-  if (cfg) *cfg = h->tile_cfg >= 0 ? h->tile_cfg : h->tuned_cfg[mode];
-  if (ms_per_launch) *ms_per_launch = h->tuned_ms[mode];
+  if (cfg)
+    *cfg = h->tile_cfg >= 0 ? h->tile_cfg : h->tuned_cfg[h->storage][mode];
+  if (ms_per_launch) *ms_per_launch = h->tuned_ms[h->storage][mode];
   return BORN_OK;
 }
 
@@ -992,6 +1216,36 @@ int born_set_tiling(born_handle *h, int cfg, int zseg) {
   h->tile_cfg = cfg;
   h->zseg = zseg;
   return BORN_OK;
+}
+
+int born_set_storage(born_handle *h, int storage) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (storage != BORN_STORE_F32 && storage != BORN_STORE_BF16 &&
+      storage != BORN_STORE_F16)
+    return fail(h, BORN_EINVAL, "unknown storage %d", storage);
+  if (storage != BORN_STORE_F32 && h->n1 % 8 != 0)
+    return fail(h, BORN_EINVAL,
+                "16-bit storage needs nx %% 8 == 0 (rows of 16-byte multiples)");
+  CK(h, cudaStreamSynchronize(h->stream));
+  if (storage != h->storage) {
+    h->storage = storage;
+    h->src_levels_valid = false;  // the levels change representation
+    h->generation++;
+    const size_t bytes = (size_t)h->n123 * 4;
+    float *lv[] = {h->s0, h->s1, h->r0, h->r1, h->f0, h->f1};
+    for (float *b : lv) CK(h, cudaMemsetAsync(b, 0, bytes, h->stream));
+    for (int b = 0; b < kNumLevelBufs; ++b) {
+      CK(h, born::launch_level_reset(h->lv_dev, b, h->stream));
+      h->wr[b] = 0;
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+  }
+  return BORN_OK;
+}
+
+int born_get_storage(const born_handle *h) {
+  return h ? h->storage : BORN_STORE_F32;
 }
 
 long long born_kernel_launches(const born_handle *h) {

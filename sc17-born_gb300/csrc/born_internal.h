@@ -12,14 +12,32 @@
 #include "../../include/born_gb300.h"
 #include "born_step.cuh"
 
+// Level buffers of a handle (index of their level records) and the device
+// words holding the maxima that 16-bit storage bounds amplitudes with.
+enum LevelBuf : int { kBufS0 = 0, kBufS1, kBufR0, kBufR1, kBufF0, kBufF1,
+                      kNumLevelBufs };
+enum StatWord : int { kStatVel1 = 0, kStatVel2, kStatRefl, kStatSrc, kStatRec,
+                      kNumStats };
+
+// Tags of the level records written by each time loop (16-bit storage):
+// every loop writes increasing tags above those of the loops whose levels it
+// reads, and clears the records of the levels it starts from zero, so the
+// tags of a replayed loop are the same as those of its first run.
+constexpr unsigned int kTagSource = 1u;
+constexpr unsigned int kTagAdjoint = 1u << 30;
+constexpr unsigned int kTagForward = 2u << 30;
+
 // Device copy of one point set (sources or receivers).
 struct DevPoints {
   int npts = 0, nt = 0;
+  int mult = 1;                          // most points sharing one cell
+  const unsigned int *absmax = nullptr;  // max |trace| word (16-bit storage)
   int zlo = 1 << 30, zhi = -1;  // planes holding points
   int *plane_off = nullptr, *cell_head = nullptr, *slot_cell = nullptr,
       *slot_index = nullptr;
   float *traces = nullptr;
   size_t traces_cap = 0;
+  std::vector<int> host_locs;  // cells as given, to recognise a repeat upload
   void release() {
     cudaFree(plane_off);
     cudaFree(cell_head);
@@ -56,10 +74,28 @@ struct born_handle {
   bool src_levels_valid = false;
   const float *host_p0 = nullptr, *host_p1 = nullptr;
   int tile_cfg = -1, zseg = 0;
-  // autotuner: best tile configuration per step mode (-1: not tuned yet)
+  // bumped whenever device buffers or point sets are reallocated, so that
+  // cached descriptors and graphs built over them can notice
+  unsigned long long generation = 0;
+  // autotuner: best tile configuration per storage and step mode (-1: not
+  // tuned yet)
   bool autotune = true;
-  int tuned_cfg[6] = {-1, -1, -1, -1, -1, -1};
-  float tuned_ms[6] = {0, 0, 0, 0, 0, 0};
+  int tuned_cfg[3][6] = {{-1, -1, -1, -1, -1, -1},
+                         {-1, -1, -1, -1, -1, -1},
+                         {-1, -1, -1, -1, -1, -1}};
+  float tuned_ms[3][6] = {};
+  // wavefield level storage (born::Storage) and, for 16-bit storage, the
+  // level records [kNumLevelBufs][2 slots][2 words], the number of writes of
+  // each level buffer since its last reset (its record slot is the parity)
+  // and the maxima words
+  int storage = 0;
+  unsigned long long *lv_dev = nullptr;
+  unsigned int *stat_dev = nullptr;
+  int wr[kNumLevelBufs] = {};
+  size_t level_bytes() const {
+    return (size_t)n123 * (storage == born::kStoreF32 ? 4 : 2);
+  }
+  int level_esize() const { return storage == born::kStoreF32 ? 4 : 2; }
   long long launches = 0;
   int ntblock = 0;
   // TMA descriptors by (buffer, tile config * 2 + kind); kind 0 = halo box,
@@ -70,6 +106,36 @@ struct born_handle {
   size_t ckpt_levels = 0, gbuf_levels = 0;
 };
 
+
+// Shared helpers (born_api.cu)
+born::PointSet born_point_view(const DevPoints &dp, int id, int ii,
+                               const std::vector<float> &tab, float scale,
+                               bool use);
+void born_base_params(born_handle *h, born::StepParams &p);
+int born_get_map(born_handle *h, const void *buf, int cfg, int kind,
+                 int esize, CUtensorMap *out);
+void born_pick_tiling(born_handle *h, int mode, bool pa, bool pb, int *cfg,
+                      int *zseg, int *tiles_x, int *tiles_y);
+int born_ensure_tuned(born_handle *h, int mode);
+
+// 16-bit storage bookkeeping (born_api.cu).  Record slots of a step that
+// reads `cur` (null: not read) and `old` and, when `write`, writes its new
+// level over `old`; born_level_written() counts that write afterwards.
+int born_level_id(const born_handle *h, const void *buf);
+born::LevelRefs born_level_refs(const born_handle *h, const void *cur,
+                                const void *old, bool write, unsigned int tag);
+void born_level_written(born_handle *h, const void *buf);
+// Before a time loop with 16-bit storage: the maxima words (velocities,
+// reflectivity, traces) and a reset of the records of the buffers the loop
+// clears.  No-op with FP32 storage.
+int born_lp_prologue(born_handle *h, cudaStream_t s, const void *const *reset,
+                     int nreset);
+// dst <- src for a level buffer (data and record).
+int born_copy_level(born_handle *h, void *dst, const void *src,
+                    unsigned int tag, cudaStream_t s);
+// Step parameters that depend on the storage: maxima words of the fields'
+// velocities (and the reflectivity for the Born coupling).
+void born_set_lp_words(born_handle *h, born::StepParams &p, int mode);
 
 // Error helpers (born_api.cu)
 int born_fail(born_handle *h, int code, const char *fmt, ...);

@@ -67,6 +67,27 @@ struct PointSet {
   int active;             // reference guard: id + 7 < nt_trace
   float scale;            // dir / jt for injection, unused for extraction
   float tab[8];           // sinc row for this step
+  // 16-bit storage: bound of |trace| (device word, float bits) and the most
+  // points sharing one cell, for the amplitude bound of an injection
+  const unsigned int *absmax;
+  int mult;
+};
+
+// Storage of the propagated wavefield levels.  Velocities, image and
+// reflectivity stay FP32; with 16-bit storage the stencil still accumulates
+// in FP32 and every stored level carries its own power-of-two scale.
+enum Storage : int { kStoreF32 = 0, kStoreBF16 = 1, kStoreF16 = 2 };
+
+// Per-level scale records (16-bit storage).  Each level buffer has two
+// record slots, used alternately by its successive writes, so that a step
+// reads the records of its current and previous levels while it fills the
+// record of the level it writes.  A slot is two words: [0] = (tag << 32) |
+// bits of max|value| (accumulated with atomicMax, the tag increasing with
+// every write within a time loop, so a stale maximum never survives), [1] =
+// bits of the level's scale (stored value = true value / scale).
+struct LevelRefs {
+  int cur, old, out;  // record slots; -1 when the level is not read/written
+  unsigned int tag;
 };
 
 // Centre-tile slots (TMA maps cm[slot] in the launch)
@@ -78,9 +99,9 @@ struct StepParams {
   int tiles_x, tiles_y, zseg;
   float c[13];             // stencil coefficients, slots as cpu_prop.cc:6-18
   float bound[kNBound];
-  // outputs (in-place over the previous level)
-  float *a_out;            // field A: source p / forward s / adjoint r / w
-  float *b_out;            // field B: forward r / adjoint s
+  // outputs (in-place over the previous level; element type per storage)
+  void *a_out;             // field A: source p / forward s / adjoint r / w
+  void *b_out;             // field B: forward r / adjoint s
   float *img_out;          // adjoint image (read through the centre ring)
   float *g_out;            // kModeModel: A s of the current level, or null
   PointSet pa;             // injection into the new level of A
@@ -88,6 +109,12 @@ struct StepParams {
                            // adjoint: injection owed to B's previous level;
                            // model: extraction from A
   unsigned int *err;       // device error word (bit 0: mbarrier wait gave up)
+  // 16-bit storage only
+  unsigned long long *lv;  // level records [slot][2]
+  LevelRefs la, lb;        // records of fields A and B this step
+  float csum;              // |c0| + 2 sum |ci|: stencil gain per unit v^2 dt^2
+  const unsigned int *vmax_a, *vmax_b;  // max v^2 dt^2 seen by A / B
+  const unsigned int *imgmax;           // max |reflectivity| (Born coupling)
 };
 
 constexpr unsigned int kErrWaitTimeout = 1u;
@@ -100,23 +127,75 @@ struct StepMaps {
   CUtensorMap cm[kNumCentre];     // centre tiles, by CentreSlot
 };
 
+// One shot of a batched launch (device memory).  `params` holds the shot's
+// static step parameters (grid, tiling, coefficients, image/g outputs, point
+// set arrays); the outputs and descriptors follow the parity of the level
+// rotation.
+struct BatchShot {
+  StepParams params;
+  void *a_out[2], *b_out[2];
+  StepMaps maps[2];
+};
+
+// Scalars that change from step to step, shared by every shot.
+struct StepVar {
+  int parity;
+  int pa_id, pa_active;
+  float pa_scale;
+  float pa_tab[8];
+  int pb_id, pb_active;
+  float pb_scale;
+  float pb_tab[8];
+  LevelRefs la, lb;  // 16-bit storage: the same rotation for every shot
+};
+
+// Batched launch over nshots shots; block_start[s] is the first CTA of shot
+// s and block_start[nshots] the total.  total_blocks == 0 only prepares the
+// kernel (its shared-memory attribute), so that a later launch can be
+// recorded into a graph.
+cudaError_t launch_step_batched(int storage, int mode, bool prop_a,
+                                bool prop_b, int tile_cfg,
+                                const BatchShot *shots, const int *block_start,
+                                int nshots, int total_blocks,
+                                const StepVar &var, cudaStream_t stream);
+
 // Host-side launch entry (defined in born_step.cu).  prop_a / prop_b say
-// which fields are propagated this step (adjoint first/last steps).
-cudaError_t launch_step(int mode, bool prop_a, bool prop_b, int tile_cfg,
-                        const StepMaps &maps, const StepParams &p,
-                        cudaStream_t stream);
+// which fields are propagated this step (adjoint first/last steps).  16-bit
+// storage supports the source, forward and adjoint modes.
+cudaError_t launch_step(int storage, int mode, bool prop_a, bool prop_b,
+                        int tile_cfg, const StepMaps &maps,
+                        const StepParams &p, cudaStream_t stream);
 
 // Which centre slots a mode reads (bit mask over CentreSlot).
 unsigned centre_mask(int mode, bool prop_a, bool prop_b);
+// Centre slots holding levels of the propagated fields (stored with the
+// field storage; the others are FP32).
+inline bool field_slot(int mode, int slot) {
+  return slot == kOldA || (slot == kOldB && mode != kModeBornAdj);
+}
 
 // Tile configurations (index -> TX, TY).
 int tile_cfg_count();
 void tile_cfg_dims(int cfg, int *tx, int *ty);
-size_t step_smem_bytes(int tile_cfg, int mode, bool prop_a, bool prop_b);
+size_t step_smem_bytes(int storage, int tile_cfg, int mode, bool prop_a,
+                       bool prop_b);
 
 // Small kernels.
-cudaError_t launch_point_inject(const PointSet &ps, int npts, float *field,
+// Adds the injection of `ps` into `field` at its points (one thread, point
+// order).  16-bit storage: decoded and re-encoded with the scale of record
+// slot `rec` of `lv`.
+cudaError_t launch_point_inject(const PointSet &ps, int npts, void *field,
+                                int storage, unsigned long long *lv, int rec,
                                 cudaStream_t stream);
+// Level records: reset both slots of buffer `buf` (zero level, scale 1), or
+// copy slot `src` into slot `dst` with a new tag.
+cudaError_t launch_level_reset(unsigned long long *lv, int buf,
+                               cudaStream_t stream);
+cudaError_t launch_level_copy(unsigned long long *lv, int dst, int src,
+                              unsigned int tag, cudaStream_t stream);
+// *out = max(*out, max |x[i]|) as float bits (out zeroed by the caller).
+cudaError_t launch_absmax(const float *x, long long n, unsigned int *out,
+                          cudaStream_t stream);
 // out[i] = a[i] / v[i] over the whole grid (image of the exact adjoint).
 cudaError_t launch_divide(const float *a, const float *v, float *out,
                           long long n, cudaStream_t stream);

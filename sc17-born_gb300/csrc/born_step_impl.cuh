@@ -1,0 +1,1038 @@
+// Templated body of the fused time-step kernels (design in born_step.cuh).
+// Included by born_step.cu (FP32 storage), born_step_bf16.cu and
+// born_step_f16.cu so that the three families compile in parallel; each
+// includer instantiates its storage types with BORN_DEFINE_STORAGE_ENTRY.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "born_step.cuh"
+
+namespace born {
+namespace {
+
+// ---------------------------------------------------------------------------
+// PTX helpers: mbarrier + TMA (sm_90+ forms, valid on sm_103a)
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile(
+      "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: gives up after ~2 s of wall time so that a lost transfer
+// turns into an error status instead of a hung GPU.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar,
+                                                  uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (uint32_t i = 0;; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63u) == 63u && global_ns() - t0 > 2000000000ull) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *tm,
+                                            int x, int y, int z,
+                                            uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::"
+      "bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(z),
+      "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ float comp(const float4 &v, int j) {
+  return j == 0 ? v.x : (j == 1 ? v.y : (j == 2 ? v.z : v.w));
+}
+__device__ __forceinline__ void set_comp(float4 &v, int j, float x) {
+  if (j == 0) v.x = x;
+  else if (j == 1) v.y = x;
+  else if (j == 2) v.z = x;
+  else v.w = x;
+}
+__device__ __forceinline__ float4 scale4(const float4 &v, float s) {
+  return make_float4(v.x * s, v.y * s, v.z * s, v.w * s);
+}
+__device__ __forceinline__ float absmax4(const float4 &v, float m) {
+  return fmaxf(fmaxf(fmaxf(m, fabsf(v.x)), fmaxf(fabsf(v.y), fabsf(v.z))),
+               fabsf(v.w));
+}
+
+// ---------------------------------------------------------------------------
+// Storage of the wavefield levels
+
+template <int ST>
+struct Store {
+  static constexpr int kBytes = ST == kStoreF32 ? 4 : 2;
+  static constexpr bool kLow = ST != kStoreF32;
+};
+
+// Four consecutive values starting at element `e` of a shared tile.
+template <int ST>
+__device__ __forceinline__ float4 ld4(const unsigned char *base, int e) {
+  if constexpr (ST == kStoreF32) {
+    return *reinterpret_cast<const float4 *>(base + 4 * e);
+  } else {
+    const uint2 u = *reinterpret_cast<const uint2 *>(base + 2 * e);
+    if constexpr (ST == kStoreBF16) {
+      // a bf16 is the upper half of the float with the same bits
+      return make_float4(__uint_as_float(u.x << 16),
+                         __uint_as_float(u.x & 0xffff0000u),
+                         __uint_as_float(u.y << 16),
+                         __uint_as_float(u.y & 0xffff0000u));
+    } else {
+      const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&u.x));
+      const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&u.y));
+      return make_float4(a.x, a.y, b.x, b.y);
+    }
+  }
+}
+
+__device__ __forceinline__ float clamp_f16(float x) {
+  // largest finite FP16; NaN passes through
+  return x > 65504.f ? 65504.f : (x < -65504.f ? -65504.f : x);
+}
+
+// Stores four consecutive values at element idx of a level (raw units).
+template <int ST>
+__device__ __forceinline__ void st4_level(void *base, long long idx,
+                                          const float4 &v) {
+  if constexpr (ST == kStoreF32) {
+    *reinterpret_cast<float4 *>(static_cast<float *>(base) + idx) = v;
+  } else {
+    uint2 u;
+    if constexpr (ST == kStoreBF16) {
+      __nv_bfloat162 a = __floats2bfloat162_rn(v.x, v.y);
+      __nv_bfloat162 b = __floats2bfloat162_rn(v.z, v.w);
+      u.x = *reinterpret_cast<unsigned int *>(&a);
+      u.y = *reinterpret_cast<unsigned int *>(&b);
+    } else {
+      __half2 a = __floats2half2_rn(clamp_f16(v.x), clamp_f16(v.y));
+      __half2 b = __floats2half2_rn(clamp_f16(v.z), clamp_f16(v.w));
+      u.x = *reinterpret_cast<unsigned int *>(&a);
+      u.y = *reinterpret_cast<unsigned int *>(&b);
+    }
+    *reinterpret_cast<uint2 *>(static_cast<unsigned short *>(base) + idx) = u;
+  }
+}
+
+template <int ST>
+__device__ __forceinline__ float ld1_level(const void *base, long long i) {
+  if constexpr (ST == kStoreF32) {
+    return static_cast<const float *>(base)[i];
+  } else if constexpr (ST == kStoreBF16) {
+    const unsigned short b = static_cast<const unsigned short *>(base)[i];
+    return __uint_as_float((unsigned int)b << 16);
+  } else {
+    return __half2float(static_cast<const __half *>(base)[i]);
+  }
+}
+
+template <int ST>
+__device__ __forceinline__ void st1_level(void *base, long long i, float v) {
+  if constexpr (ST == kStoreF32) {
+    static_cast<float *>(base)[i] = v;
+  } else if constexpr (ST == kStoreBF16) {
+    static_cast<__nv_bfloat16 *>(base)[i] = __float2bfloat16_rn(v);
+  } else {
+    static_cast<__half *>(base)[i] = __float2half_rn(clamp_f16(v));
+  }
+}
+
+// Stored values are kept at or below 2^15 in magnitude (FP16 overflows
+// above 65504): the scale of a new level is the power of two
+// 2^(ceil(log2 bound) - 15) for a bound on its magnitude.
+constexpr int kScaleHeadroomLog2 = 15;
+
+__device__ __forceinline__ float pow2_scale_for(float bound) {
+  if (!(bound > 0.f) || bound > 3.0e38f) return 1.f;
+  const unsigned int b = __float_as_uint(bound);
+  int e = (int)((b >> 23) & 0xffu) - 127;       // floor(log2) (normal floats)
+  if ((b & 0x7fffffu) != 0u || e < -126) e += 1;  // round up to a power of two
+  e -= kScaleHeadroomLog2;
+  e = e < -120 ? -120 : (e > 120 ? 120 : e);
+  return __uint_as_float((unsigned int)(e + 127) << 23);
+}
+
+__device__ __forceinline__ float rec_max(const unsigned long long *lv, int r) {
+  return r < 0 ? 0.f
+               : __uint_as_float((unsigned int)(lv[2 * r] & 0xffffffffull));
+}
+__device__ __forceinline__ float rec_scale(const unsigned long long *lv,
+                                           int r) {
+  return r < 0 ? 1.f
+               : __uint_as_float((unsigned int)(lv[2 * r + 1] & 0xffffffffull));
+}
+
+// Bound of one step's injection: |trace| * |dir/jt| * sum |tab| per point,
+// times the most points sharing a cell.
+__device__ __forceinline__ float inject_bound(const PointSet &ps) {
+  if (!ps.active || !ps.absmax) return 0.f;
+  float t = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) t += fabsf(ps.tab[k]);
+  return __uint_as_float(*ps.absmax) * fabsf(ps.scale) * t * (float)ps.mult;
+}
+
+// ---------------------------------------------------------------------------
+// Reference arithmetic (FP32 storage)
+
+// Leapfrog update of cpuProp::prop (cpu_prop.cc:233-248): v*S + p + p - old,
+// every operation separately rounded (no FMA contraction).
+__device__ __forceinline__ float leapfrog(float vel, float s, float p,
+                                          float old) {
+  return __fsub_rn(__fadd_rn(__fadd_rn(__fmul_rn(vel, s), p), p), old);
+}
+
+// dir/jt * (t0 v0 + ... + t7 v7), cpu_prop.cc:169-177 / 186-194
+__device__ __forceinline__ float point_value(const PointSet &ps, int idx) {
+  const float *v = ps.traces + (long long)idx * ps.nt_trace + ps.id;
+  float s = __fmul_rn(ps.tab[0], v[0]);
+#pragma unroll
+  for (int k = 1; k < 8; ++k) s = __fadd_rn(s, __fmul_rn(ps.tab[k], v[k]));
+  return __fmul_rn(ps.scale, s);
+}
+
+// Adds the injection of every point lying on this thread's 4 cells of row
+// gy, plane z, in point order.  Uniform early-out when the plane is empty.
+__device__ __forceinline__ void inject_row(const PointSet &ps, int n1, int n2,
+                                           int z, int gy, int gx, float4 &v) {
+  if (z < ps.zlo || z > ps.zhi) return;
+  const int off = ps.plane_off[z];
+  if (off < 0) return;
+  const int4 h = *reinterpret_cast<const int4 *>(ps.cell_head + off +
+                                                 (long long)gy * n1 + gx);
+  const int hh[4] = {h.x, h.y, h.z, h.w};
+  const long long cell0 = ((long long)z * n2 + gy) * n1 + gx;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    if (hh[j] < 0) continue;
+    float a = comp(v, j);
+    for (int s = hh[j]; s < ps.npts && ps.slot_cell[s] == (int)(cell0 + j);
+         ++s)
+      a = __fadd_rn(a, point_value(ps, ps.slot_index[s]));
+    set_comp(v, j, a);
+  }
+}
+
+// rec[idx][id+k] += v * t[k] at every point on this thread's cells
+// (cpu_prop.cc:205-212).
+__device__ __forceinline__ void extract_row(const PointSet &ps, int n1, int n2,
+                                            int z, int gy, int gx,
+                                            const float4 &v) {
+  if (z < ps.zlo || z > ps.zhi) return;
+  const int off = ps.plane_off[z];
+  if (off < 0) return;
+  const int4 h = *reinterpret_cast<const int4 *>(ps.cell_head + off +
+                                                 (long long)gy * n1 + gx);
+  const int hh[4] = {h.x, h.y, h.z, h.w};
+  const long long cell0 = ((long long)z * n2 + gy) * n1 + gx;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    if (hh[j] < 0) continue;
+    const float a = comp(v, j);
+    for (int s = hh[j]; s < ps.npts && ps.slot_cell[s] == (int)(cell0 + j);
+         ++s) {
+      float *r = ps.traces + (long long)ps.slot_index[s] * ps.nt_trace + ps.id;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) r[k] = __fadd_rn(r[k], __fmul_rn(a, ps.tab[k]));
+    }
+  }
+}
+
+__device__ __forceinline__ void st4(float *p, const float4 &v) {
+  *reinterpret_cast<float4 *>(p) = v;
+}
+
+// Stencil sums of this thread's 4 consecutive cells (x .. x+3) of one row,
+// from a TMA box (x/y neighbours) and the register z window.  Each cell's
+// sum is formed in the reference order of cpuProp::prop (cpu_prop.cc:235-247):
+// C0 p, then the x pairs, the y pairs and the z pairs, every product and sum
+// separately rounded; the four cells advance together so that every shared
+// load is a float4 (3 for the x window, 2 per y offset).
+template <int BX>
+__device__ __forceinline__ float4 stencil4(const float *box, int brow,
+                                           int bcol, const float4 (&q)[9],
+                                           const float *c, float4 &center) {
+  const float *r = box + brow * BX + bcol;
+  float w[12];
+  {
+    const float4 L = *reinterpret_cast<const float4 *>(r - 4);
+    const float4 M = *reinterpret_cast<const float4 *>(r);
+    const float4 R = *reinterpret_cast<const float4 *>(r + 4);
+    w[0] = L.x; w[1] = L.y; w[2] = L.z; w[3] = L.w;
+    w[4] = M.x; w[5] = M.y; w[6] = M.z; w[7] = M.w;
+    w[8] = R.x; w[9] = R.y; w[10] = R.z; w[11] = R.w;
+    center = M;
+  }
+  float s[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    s[j] = __fmul_rn(c[0], w[4 + j]);
+    s[j] = __fadd_rn(s[j], __fmul_rn(c[2], __fadd_rn(w[3 + j], w[5 + j])));
+    s[j] = __fadd_rn(s[j], __fmul_rn(c[5], __fadd_rn(w[2 + j], w[6 + j])));
+    s[j] = __fadd_rn(s[j], __fmul_rn(c[8], __fadd_rn(w[1 + j], w[7 + j])));
+    s[j] = __fadd_rn(s[j], __fmul_rn(c[11], __fadd_rn(w[0 + j], w[8 + j])));
+  }
+  const int cy[4] = {3, 6, 9, 12}, cz[4] = {1, 4, 7, 10};
+#pragma unroll
+  for (int m = 1; m <= 4; ++m) {
+    const float4 u = *reinterpret_cast<const float4 *>(r - m * BX);
+    const float4 d = *reinterpret_cast<const float4 *>(r + m * BX);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      s[j] = __fadd_rn(s[j], __fmul_rn(c[cy[m - 1]],
+                                       __fadd_rn(comp(u, j), comp(d, j))));
+  }
+#pragma unroll
+  for (int m = 1; m <= 4; ++m)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      s[j] = __fadd_rn(
+          s[j], __fmul_rn(c[cz[m - 1]],
+                          __fadd_rn(comp(q[4 - m], j), comp(q[4 + m], j))));
+  return make_float4(s[0], s[1], s[2], s[3]);
+}
+
+// The same sums over 16-bit stored values (raw units: the caller applies the
+// level's scale), with fused multiply-adds: the reduced-precision path is
+// judged by its error against FP64, not by bit equality.
+template <int BX, int ST>
+__device__ __forceinline__ float4 stencil4_lp(const unsigned char *box,
+                                              int brow, int bcol,
+                                              const float4 (&q)[9],
+                                              const float *c, float4 &center) {
+  const int e = brow * BX + bcol;
+  float w[12];
+  {
+    const float4 L = ld4<ST>(box, e - 4);
+    const float4 M = ld4<ST>(box, e);
+    const float4 R = ld4<ST>(box, e + 4);
+    w[0] = L.x; w[1] = L.y; w[2] = L.z; w[3] = L.w;
+    w[4] = M.x; w[5] = M.y; w[6] = M.z; w[7] = M.w;
+    w[8] = R.x; w[9] = R.y; w[10] = R.z; w[11] = R.w;
+    center = M;
+  }
+  float s[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    s[j] = c[0] * w[4 + j];
+    s[j] = fmaf(c[2], w[3 + j] + w[5 + j], s[j]);
+    s[j] = fmaf(c[5], w[2 + j] + w[6 + j], s[j]);
+    s[j] = fmaf(c[8], w[1 + j] + w[7 + j], s[j]);
+    s[j] = fmaf(c[11], w[0 + j] + w[8 + j], s[j]);
+  }
+  const int cy[4] = {3, 6, 9, 12}, cz[4] = {1, 4, 7, 10};
+#pragma unroll
+  for (int m = 1; m <= 4; ++m) {
+    const float4 u = ld4<ST>(box, e - m * BX);
+    const float4 d = ld4<ST>(box, e + m * BX);
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      s[j] = fmaf(c[cy[m - 1]], comp(u, j) + comp(d, j), s[j]);
+  }
+#pragma unroll
+  for (int m = 1; m <= 4; ++m)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      s[j] = fmaf(c[cz[m - 1]], comp(q[4 - m], j) + comp(q[4 + m], j), s[j]);
+  return make_float4(s[0], s[1], s[2], s[3]);
+}
+
+// ---------------------------------------------------------------------------
+// Compile-time description of a mode
+
+template <int MODE, bool PA, bool PB>
+struct ModeTraits {
+  static constexpr bool kTwoField = (MODE == kModeForward ||
+                                     MODE == kModeBornLin ||
+                                     MODE == kModeAdjoint);
+  static constexpr bool kBoxA = PA;
+  static constexpr bool kBoxB = kTwoField && PB;
+  static constexpr int kNF = (kBoxA ? 1 : 0) + (kBoxB ? 1 : 0);
+  static constexpr unsigned kMask =
+      MODE == kModeSource || MODE == kModeModel
+          ? (1u << kOldA) | (1u << kVelA)
+      : MODE == kModeForward || MODE == kModeBornLin
+          ? (1u << kOldA) | (1u << kOldB) | (1u << kVelA) | (1u << kImg)
+      : MODE == kModeAdjoint
+          ? (1u << kOldA) | (1u << kOldB) | (1u << kImg) |
+                (PA ? (1u << kVelA) : 0u) | (PB ? (1u << kVelB) : 0u)
+          : /* kModeBornAdj: OldB slot carries g = A s */
+          (1u << kOldA) | (1u << kOldB) | (1u << kVelA) | (1u << kImg);
+  static constexpr bool kDampA = MODE != kModeSource;
+  static constexpr bool kDampB = MODE == kModeForward || MODE == kModeBornLin;
+};
+
+// Shared-memory geometry of one tile shape for field elements of EB bytes.
+// TMA copies of 16-bit rows must start at an x that is a multiple of 8
+// elements; the interior starts at x = 4, so 16-bit centre tiles are copied
+// from x0 - 4 with 8 extra columns (the halo boxes already start there).
+template <int TX, int TY, int EB>
+struct Tile {
+  static constexpr int kBX = TX + 2 * kRadius, kBY = TY + 2 * kRadius;
+  static constexpr int kThreads = (TX / 4) * TY;
+  static constexpr int kZCols = EB == 4 ? TX : TX + 2 * kRadius;
+  static constexpr int kZOff = EB == 4 ? 0 : kRadius;
+  static constexpr int kZRaw = kZCols * TY * EB;  // bytes one copy delivers
+  static constexpr int kZBytes = (kZRaw + 127) / 128 * 128;
+  static constexpr int kBoxRaw = kBX * kBY * EB;
+  static constexpr int kBoxBytes = (kBoxRaw + 127) / 128 * 128;
+  static constexpr int kCRaw = TX * TY * 4;       // FP32 centre tile
+  static constexpr int kCBytes = (kCRaw + 127) / 128 * 128;
+};
+
+// centre slots that hold levels of the propagated fields (field storage)
+template <int MODE>
+__host__ __device__ constexpr bool fslot(int slot) {
+  return slot == kOldA || (slot == kOldB && MODE != kModeBornAdj);
+}
+template <int MODE, class T>
+__host__ __device__ constexpr int slot_raw(int slot) {
+  return fslot<MODE>(slot) ? T::kZRaw : T::kCRaw;
+}
+template <int MODE, class T>
+__host__ __device__ constexpr int slot_bytes(int slot) {
+  return fslot<MODE>(slot) ? T::kZBytes : T::kCBytes;
+}
+// byte offset of a centre slot inside the centre part of an output stage
+template <int MODE, unsigned MASK, class T>
+__host__ __device__ constexpr int slot_off(int slot) {
+  int off = 0;
+  for (int s = 0; s < slot; ++s)
+    if (MASK & (1u << s)) off += slot_bytes<MODE, T>(s);
+  return off;
+}
+template <int MODE, unsigned MASK, class T>
+__host__ __device__ constexpr int centre_bytes(bool raw) {
+  int b = 0;
+  for (int s = 0; s < kNumCentre; ++s)
+    if (MASK & (1u << s))
+      b += raw ? slot_raw<MODE, T>(s) : slot_bytes<MODE, T>(s);
+  return b;
+}
+
+template <int ST, int MODE, bool PA, bool PB, int TX, int TY>
+struct Layout {
+  using M = ModeTraits<MODE, PA, PB>;
+  using T = Tile<TX, TY, Store<ST>::kBytes>;
+  static constexpr int kZStage = M::kNF * T::kZBytes;
+  static constexpr int kOStage =
+      M::kNF * T::kBoxBytes + centre_bytes<MODE, M::kMask, T>(false);
+  static constexpr uint32_t kZTx = M::kNF * T::kZRaw;
+  static constexpr uint32_t kOTx =
+      M::kNF * T::kBoxRaw + centre_bytes<MODE, M::kMask, T>(true);
+  static constexpr size_t kSmem =
+      (size_t)kZStages * kZStage + (size_t)kOStages * kOStage + 128;
+};
+
+// Scales of one step's levels (16-bit storage), shared by the CTA.
+struct StepScales {
+  float cur_a, old_a, inv_new_a, cur_b, old_b, inv_new_b;
+};
+
+// One CTA's work: xy tile `tile`, z segment `seg`, with the TMA descriptors
+// `mp` (kernel parameter space, or global memory in the batched launch) and
+// the step parameters `p`.
+template <int ST, int MODE, bool PA, bool PB, int TX, int TY>
+__device__ __forceinline__ void step_body(const StepMaps *mp,
+                                          const StepParams &p, int tile,
+                                          int seg) {
+  const StepMaps &maps = *mp;
+  using M = ModeTraits<MODE, PA, PB>;
+  using T = Tile<TX, TY, Store<ST>::kBytes>;
+  using LY = Layout<ST, MODE, PA, PB, TX, TY>;
+  constexpr bool LP = Store<ST>::kLow;
+  constexpr int NF = M::kNF;
+  constexpr int BX = T::kBX;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t zbars[kZStages];
+  __shared__ __align__(8) uint64_t obars[kOStages];
+  __shared__ int abort_flag;
+  __shared__ float s_bound[kNBound];
+  __shared__ StepScales s_sc;
+  __shared__ unsigned int s_mx[2];
+  // TMA destinations need 128-byte alignment: align the dynamic base here
+  // (the launch reserves 128 spare bytes for this)
+  unsigned char *smem =
+      smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  // z ring: centre tiles of the current levels, one per new plane
+  unsigned char *zring = smem;
+  // output ring: halo boxes and per-cell inputs of the output plane
+  unsigned char *oring = smem + kZStages * LY::kZStage;
+
+  const int tid = threadIdx.x;
+  const int lx = tid % (TX / 4), ly = tid / (TX / 4);
+  const int tx = tile % p.tiles_x, ty = tile / p.tiles_x;
+  const int x0 = kRadius + tx * TX, y0 = kRadius + ty * TY;
+  const int z0 = kRadius + seg * p.zseg;
+  const int z1 = min(z0 + p.zseg, p.n3 - kRadius);
+  if (z0 >= z1) return;  // uniform over the CTA
+  const int n1 = p.n1, n2 = p.n2, n3 = p.n3;
+  const long long n12 = (long long)n1 * n2;
+  const int gx = x0 + 4 * lx, gy = y0 + ly;
+  const bool valid = (gx < n1 - kRadius) && (gy < n2 - kRadius);
+  // x of the field centre copies (16-bit rows start 4 columns early)
+  const int xz = x0 - T::kZOff;
+
+  // taper: distance to the interior faces in x/y per cell (cpu_prop.cc:146-151)
+  int exy[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int x = gx + j;
+    exy[j] = min(min(x - 4, n1 - 4 - x), min(gy - 4, n2 - 4 - gy));
+  }
+
+  if (tid == 0) {
+    for (int s = 0; s < kZStages; ++s) mbar_init(&zbars[s], 1);
+    for (int s = 0; s < kOStages; ++s) mbar_init(&obars[s], 1);
+    // a wait elsewhere already gave up: the whole CTA leaves untouched
+    abort_flag = *reinterpret_cast<volatile unsigned int *>(p.err) != 0u;
+    mbar_fence_init();
+    if constexpr (LP) {
+      // scales of the levels read, and of the levels written from a bound
+      // on their magnitude: |v S| <= vmax csum max|cur|, plus 2 max|cur|,
+      // max|old| and the injections (every CTA computes the same values)
+      const float ga = __uint_as_float(*p.vmax_a) * p.csum + 2.f;
+      const float ma = rec_max(p.lv, p.la.cur), mo = rec_max(p.lv, p.la.old);
+      const float ba = ga * ma + mo + inject_bound(p.pa);
+      s_sc.cur_a = rec_scale(p.lv, p.la.cur);
+      s_sc.old_a = rec_scale(p.lv, p.la.old);
+      const float na = pow2_scale_for(ba);
+      s_sc.inv_new_a = 1.f / na;  // exact: a power of two
+      s_sc.cur_b = s_sc.old_b = s_sc.inv_new_b = 1.f;
+      float nb = 1.f;
+      if (M::kTwoField) {
+        const float gb = __uint_as_float(*p.vmax_b) * p.csum + 2.f;
+        float bb = gb * rec_max(p.lv, p.lb.cur) + rec_max(p.lv, p.lb.old);
+        if (MODE == kModeAdjoint) bb += inject_bound(p.pb);  // pending, old
+        if (MODE == kModeForward)  // Born coupling 1e-6 s_new img
+          bb += 1e-6f * ba * __uint_as_float(*p.imgmax);
+        s_sc.cur_b = rec_scale(p.lv, p.lb.cur);
+        s_sc.old_b = rec_scale(p.lv, p.lb.old);
+        nb = pow2_scale_for(bb);
+        s_sc.inv_new_b = 1.f / nb;
+      }
+      if (tile == 0 && seg == 0) {  // one CTA records the new scales
+        if (p.la.out >= 0) p.lv[2 * p.la.out + 1] = __float_as_uint(na);
+        if (M::kTwoField && p.lb.out >= 0)
+          p.lv[2 * p.lb.out + 1] = __float_as_uint(nb);
+      }
+      s_mx[0] = 0u;
+      s_mx[1] = 0u;
+    }
+  }
+  if (tid < kNBound) s_bound[tid] = p.bound[tid];
+  __syncthreads();
+  if (abort_flag) return;  // uniform: read after the barrier
+
+  const int K = (z1 - z0) + 2 * kRadius;  // z-window planes z0-4 .. z1+3
+  const int J = z1 - z0;                  // output planes
+  auto issue_z = [&](int k) {
+    const int plane = z0 - kRadius + k;
+    const int st = k % kZStages;
+    mbar_expect_tx(&zbars[st], LY::kZTx);
+    unsigned char *dst = zring + st * LY::kZStage;
+    if (M::kBoxA) tma_load_3d(dst, &maps.zc_a, xz, y0, plane, &zbars[st]);
+    if (M::kBoxB)
+      tma_load_3d(dst + (M::kBoxA ? T::kZBytes : 0), &maps.zc_b, xz, y0,
+                  plane, &zbars[st]);
+  };
+  auto issue_out = [&](int j) {
+    const int plane = z0 + j;
+    const int st = j % kOStages;
+    mbar_expect_tx(&obars[st], LY::kOTx);
+    unsigned char *dst = oring + st * LY::kOStage;
+    if (M::kBoxA)
+      tma_load_3d(dst, &maps.box_a, x0 - kRadius, y0 - kRadius, plane,
+                  &obars[st]);
+    if (M::kBoxB)
+      tma_load_3d(dst + (M::kBoxA ? T::kBoxBytes : 0), &maps.box_b,
+                  x0 - kRadius, y0 - kRadius, plane, &obars[st]);
+    unsigned char *cdst = dst + NF * T::kBoxBytes;
+#pragma unroll
+    for (int s = 0; s < kNumCentre; ++s)
+      if (M::kMask & (1u << s)) {
+        tma_load_3d(cdst + slot_off<MODE, M::kMask, T>(s), &maps.cm[s],
+                    fslot<MODE>(s) ? xz : x0, y0, plane, &obars[st]);
+      }
+  };
+  if (tid == 0) {
+    if (NF > 0)
+      for (int k = 0; k < min(K, kZStages); ++k) issue_z(k);
+    for (int j = 0; j < min(J, kOStages); ++j) issue_out(j);
+  }
+
+  float4 qa[9], qb[9];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    qa[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    qb[i] = qa[i];
+  }
+  const int brow = ly + kRadius, bcol = 4 * lx + kRadius;
+  const int fe = ly * T::kZCols + T::kZOff + 4 * lx;  // field centre element
+  const int ce = ly * TX + 4 * lx;                     // FP32 centre element
+  float mx_a = 0.f, mx_b = 0.f;  // max |stored value| (16-bit storage)
+
+  for (int k = 0; k < K; ++k) {
+    const int st = k % kZStages;
+    const int j = k - 2 * kRadius;       // output index once k >= 8
+    const int zo = z0 + j;
+    const long long idx = (long long)zo * n12 + (long long)gy * n1 + gx;
+
+    bool ok = true;
+    if (NF > 0) {
+      ok = mbar_wait_bounded(&zbars[st], (uint32_t)((k / kZStages) & 1));
+      // newest plane's centre enters the z window
+      const unsigned char *sa = zring + st * LY::kZStage;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        qa[i] = qa[i + 1];
+        qb[i] = qb[i + 1];
+      }
+      if (M::kBoxA) qa[8] = ld4<ST>(sa, fe);
+      if (M::kBoxB) qb[8] = ld4<ST>(sa + (M::kBoxA ? T::kZBytes : 0), fe);
+    }
+
+    if (j >= 0 && ok) {
+      const int os = j % kOStages;
+      ok = mbar_wait_bounded(&obars[os], (uint32_t)((j / kOStages) & 1));
+      const unsigned char *ost = oring + os * LY::kOStage;
+      const unsigned char *cst = ost + NF * T::kBoxBytes;
+      auto centre = [&](int slot) {
+        const unsigned char *b = cst + slot_off<MODE, M::kMask, T>(slot);
+        return fslot<MODE>(slot) ? ld4<ST>(b, fe) : ld4<kStoreF32>(b, ce);
+      };
+      const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 oa = (M::kMask & (1u << kOldA)) ? centre(kOldA) : zero4;
+      float4 ob = (M::kMask & (1u << kOldB)) ? centre(kOldB) : zero4;
+      if constexpr (LP) {  // true values of the previous levels
+        oa = scale4(oa, s_sc.old_a);
+        ob = scale4(ob, s_sc.old_b);
+      }
+      const float4 va = (M::kMask & (1u << kVelA)) ? centre(kVelA) : zero4;
+      const float4 vb = (M::kMask & (1u << kVelB)) ? centre(kVelB)
+                        : (MODE == kModeForward || MODE == kModeBornLin) ? va
+                                                                        : zero4;
+      const float4 im = (M::kMask & (1u << kImg)) ? centre(kImg) : zero4;
+
+      const unsigned char *box_a = ost;
+      const unsigned char *box_b = box_a + (M::kBoxA ? T::kBoxBytes : 0);
+      const int ez = min(zo - 4, n3 - 4 - zo);
+
+      // pending source injection owed to the previous level of s (adjoint)
+      if (MODE == kModeAdjoint && PB && p.pb.active && valid && ok)
+        inject_row(p.pb, n1, n2, zo, gy, gx, ob);
+
+      float4 na = oa, nb = ob, ga = zero4, sb = zero4, ca = zero4, cb = zero4;
+      if constexpr (LP) {
+        if (M::kBoxA) {
+          ga = scale4(stencil4_lp<BX, ST>(box_a, brow, bcol, qa, p.c, ca),
+                      s_sc.cur_a);
+          ca = scale4(ca, s_sc.cur_a);
+        }
+        if (M::kBoxB) {
+          sb = scale4(stencil4_lp<BX, ST>(box_b, brow, bcol, qb, p.c, cb),
+                      s_sc.cur_b);
+          cb = scale4(cb, s_sc.cur_b);
+        }
+      } else {
+        if (M::kBoxA)
+          ga = stencil4<BX>(reinterpret_cast<const float *>(box_a), brow,
+                            bcol, qa, p.c, ca);
+        if (M::kBoxB)
+          sb = stencil4<BX>(reinterpret_cast<const float *>(box_b), brow,
+                            bcol, qb, p.c, cb);
+      }
+      float bj[4];
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj) {
+        const int e = min(exy[jj], ez);
+        const float b = (e >= 0 && e < kNBound) ? s_bound[e] : 1.0f;
+        bj[jj] = b;
+        if (M::kBoxA) {
+          float old = comp(oa, jj);
+          if (M::kDampA) old = __fmul_rn(old, b);
+          float v = LP ? fmaf(comp(va, jj), comp(ga, jj),
+                              comp(ca, jj) + comp(ca, jj) - old)
+                       : leapfrog(comp(va, jj), comp(ga, jj), comp(ca, jj),
+                                  old);
+          // the adjoint of the linearised step injects its data before the
+          // taper (see below); every other tapered mode tapers here
+          if (MODE != kModeBornAdj && M::kDampA) v = __fmul_rn(v, b);
+          set_comp(na, jj, v);
+        } else if (MODE == kModeAdjoint) {
+          // receiver level not propagated (it == 0): both damping passes
+          set_comp(na, jj, __fmul_rn(__fmul_rn(comp(oa, jj), b), b));
+        }
+        if (M::kBoxB) {
+          float old = comp(ob, jj);
+          if (M::kDampB) old = __fmul_rn(old, b);
+          float v = LP ? fmaf(comp(vb, jj), comp(sb, jj),
+                              comp(cb, jj) + comp(cb, jj) - old)
+                       : leapfrog(comp(vb, jj), comp(sb, jj), comp(cb, jj),
+                                  old);
+          // linearised Born: scattering source m (A s) inside the taper
+          if (MODE == kModeBornLin)
+            v = __fadd_rn(v, __fmul_rn(comp(im, jj), comp(ga, jj)));
+          if (M::kDampB) v = __fmul_rn(v, b);
+          set_comp(nb, jj, v);
+        }
+      }
+
+      // stores a level of field A or B (scaled and tracked with 16-bit
+      // storage)
+      auto store_a = [&](const float4 &v) {
+        if constexpr (LP) {
+          mx_a = absmax4(v, mx_a);
+          st4_level<ST>(p.a_out, idx, scale4(v, s_sc.inv_new_a));
+        } else {
+          st4_level<ST>(p.a_out, idx, v);
+        }
+      };
+      auto store_b = [&](const float4 &v) {
+        if constexpr (LP) {
+          mx_b = absmax4(v, mx_b);
+          st4_level<ST>(p.b_out, idx, scale4(v, s_sc.inv_new_b));
+        } else {
+          st4_level<ST>(p.b_out, idx, v);
+        }
+      };
+
+      if (valid && ok) {
+        if (MODE == kModeBornAdj) {
+          // w = b (v A w + 2w - b w_old + v E^T d); image += (A s) w
+          float4 inj = zero4;
+          if (p.pa.active) inject_row(p.pa, n1, n2, zo, gy, gx, inj);
+          float4 ni;
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            const float w = __fmul_rn(
+                __fadd_rn(comp(na, jj), __fmul_rn(comp(va, jj), comp(inj, jj))),
+                bj[jj]);
+            set_comp(na, jj, w);
+            set_comp(ni, jj, __fadd_rn(comp(im, jj), __fmul_rn(comp(ob, jj), w)));
+          }
+          st4(p.img_out + idx, ni);
+          store_a(na);
+        } else {
+          if (p.pa.active) inject_row(p.pa, n1, n2, zo, gy, gx, na);
+          if (MODE == kModeForward) {
+            // Born coupling r += 1e-6 s img, then extraction from r
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj)
+              set_comp(nb, jj,
+                       __fadd_rn(comp(nb, jj),
+                                 __fmul_rn(__fmul_rn(1e-6f, comp(na, jj)),
+                                           comp(im, jj))));
+          }
+          if (MODE == kModeForward || MODE == kModeBornLin) {
+            if (p.pb.active) extract_row(p.pb, n1, n2, zo, gy, gx, nb);
+            store_a(na);
+            store_b(nb);
+          } else if (MODE == kModeAdjoint) {
+            // s is the new level when propagated, else the stored one
+            float4 ni;
+            ni.x = __fadd_rn(im.x, __fmul_rn(nb.x, na.x));
+            ni.y = __fadd_rn(im.y, __fmul_rn(nb.y, na.y));
+            ni.z = __fadd_rn(im.z, __fmul_rn(nb.z, na.z));
+            ni.w = __fadd_rn(im.w, __fmul_rn(nb.w, na.w));
+            st4(p.img_out + idx, ni);
+            store_a(na);
+            if (PB) store_b(nb);
+          } else {  // source, model
+            if (MODE == kModeModel) {
+              if (p.pb.active) extract_row(p.pb, n1, n2, zo, gy, gx, na);
+              if (p.g_out) st4(p.g_out + idx, ga);
+            }
+            store_a(na);
+          }
+        }
+      }
+    }
+    if (!ok) {
+      abort_flag = 1;
+      atomicOr(p.err, kErrWaitTimeout);
+    }
+
+    __syncthreads();
+    if (abort_flag) break;
+    if (tid == 0) {
+      fence_proxy_async();
+      if (NF > 0 && k + kZStages < K) issue_z(k + kZStages);
+      if (j >= 0 && j + kOStages < J) issue_out(j + kOStages);
+    }
+  }
+
+  if (abort_flag && tid == 0) {
+    // drain whatever is still in flight (bounded) before the CTA retires
+    for (int s = 0; s < kZStages + kOStages; ++s) {
+      uint64_t *b = s < kZStages ? &zbars[s] : &obars[s - kZStages];
+      const uint64_t t0 = global_ns();
+      while (!mbar_try_wait(b, 0) && !mbar_try_wait(b, 1) &&
+             global_ns() - t0 < 100000000ull) {
+      }
+    }
+  }
+
+  if constexpr (LP) {
+    // the level maxima: warp, then CTA, then one tagged atomic per CTA
+    const unsigned int wa = __reduce_max_sync(0xffffffffu, __float_as_uint(mx_a));
+    const unsigned int wb = __reduce_max_sync(0xffffffffu, __float_as_uint(mx_b));
+    if ((tid & 31) == 0) {
+      atomicMax(&s_mx[0], wa);
+      atomicMax(&s_mx[1], wb);
+    }
+    __syncthreads();
+    if (tid == 0 && !abort_flag) {
+      if (p.la.out >= 0)
+        atomicMax(&p.lv[2 * p.la.out],
+                  ((unsigned long long)p.la.tag << 32) | s_mx[0]);
+      if (M::kTwoField && PB && p.lb.out >= 0)
+        atomicMax(&p.lv[2 * p.lb.out],
+                  ((unsigned long long)p.lb.tag << 32) | s_mx[1]);
+    }
+  }
+}
+
+template <int ST, int MODE, bool PA, bool PB, int TX, int TY>
+__global__ void __launch_bounds__(Tile<TX, TY, 4>::kThreads)
+    step_kernel(const __grid_constant__ StepMaps maps, const StepParams p) {
+  step_body<ST, MODE, PA, PB, TX, TY>(&maps, p, blockIdx.x, blockIdx.y);
+}
+
+// Batched launch: blockIdx.x enumerates the CTAs of every shot in turn
+// (block_start[s] .. block_start[s+1]-1 belong to shot s); each shot brings
+// its own grid, buffers, point sets and TMA descriptors (one set per level
+// parity), the step-varying scalars come in `var`.
+template <int ST, int MODE, bool PA, bool PB, int TX, int TY>
+__global__ void __launch_bounds__(Tile<TX, TY, 4>::kThreads)
+    step_kernel_batched(const BatchShot *shots, const int *block_start,
+                        int nshots, const StepVar var) {
+  __shared__ StepParams sp;
+  __shared__ int s_shot, s_local;
+  if (threadIdx.x == 0) {
+    int lo = 0, hi = nshots - 1;  // last shot whose start <= blockIdx.x
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (block_start[mid] <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+    }
+    s_shot = lo;
+    s_local = (int)blockIdx.x - block_start[lo];
+    const BatchShot &b = shots[lo];
+    sp = b.params;
+    sp.a_out = b.a_out[var.parity];
+    sp.b_out = b.b_out[var.parity];
+    sp.pa.id = var.pa_id;
+    sp.pa.active = var.pa_active && sp.pa.npts > 0;
+    sp.pa.scale = var.pa_scale;
+    sp.pb.id = var.pb_id;
+    sp.pb.active = var.pb_active && sp.pb.npts > 0;
+    sp.pb.scale = var.pb_scale;
+    for (int k = 0; k < 8; ++k) {
+      sp.pa.tab[k] = var.pa_tab[k];
+      sp.pb.tab[k] = var.pb_tab[k];
+    }
+    sp.la = var.la;
+    sp.lb = var.lb;
+  }
+  __syncthreads();
+  const BatchShot &b = shots[s_shot];
+  const int ntiles = sp.tiles_x * sp.tiles_y;
+  step_body<ST, MODE, PA, PB, TX, TY>(&b.maps[var.parity], sp,
+                                      s_local % ntiles, s_local / ntiles);
+}
+
+// ---------------------------------------------------------------------------
+// Host side: launches and dispatch for one storage type
+
+struct TileCfg {
+  int tx, ty;
+};
+constexpr TileCfg kTileCfgs[] = {{64, 16}, {32, 16}, {32, 32}, {64, 8},
+                                 {32, 8}};
+constexpr int kNumTileCfgs = sizeof(kTileCfgs) / sizeof(kTileCfgs[0]);
+
+template <int ST, int MODE, bool PA, bool PB, int TX, int TY>
+cudaError_t launch_t(const StepMaps &maps, const StepParams &p,
+                     cudaStream_t stream) {
+  using T = Tile<TX, TY, 4>;
+  const size_t smem = Layout<ST, MODE, PA, PB, TX, TY>::kSmem;
+  auto kern = step_kernel<ST, MODE, PA, PB, TX, TY>;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(
+        kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  const int nseg = (p.n3 - 2 * kRadius + p.zseg - 1) / p.zseg;
+  dim3 grid(p.tiles_x * p.tiles_y, nseg);
+  kern<<<grid, T::kThreads, smem, stream>>>(maps, p);
+  return cudaGetLastError();
+}
+
+template <int ST, int MODE, bool PA, bool PB, int TX, int TY>
+cudaError_t launch_t_batched(const BatchShot *shots, const int *block_start,
+                             int nshots, int total, const StepVar &var,
+                             cudaStream_t stream) {
+  using T = Tile<TX, TY, 4>;
+  const size_t smem = Layout<ST, MODE, PA, PB, TX, TY>::kSmem;
+  auto kern = step_kernel_batched<ST, MODE, PA, PB, TX, TY>;
+  static bool configured = false;
+  if (!configured) {
+    cudaError_t e = cudaFuncSetAttribute(
+        kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    configured = true;
+  }
+  if (total == 0) return cudaSuccess;  // configuration only
+  kern<<<total, T::kThreads, smem, stream>>>(shots, block_start, nshots, var);
+  return cudaGetLastError();
+}
+
+// Dispatch over (mode, pa, pb) for one tile shape; F::go is instantiated
+// for every variant (FP32 storage: every mode; 16-bit: source, forward and
+// adjoint).
+template <int ST, int TX, int TY, class F>
+auto dispatch(int mode, bool pa, bool pb, F f) {
+  if constexpr (ST == kStoreF32) {
+    switch (mode) {
+      case kModeModel: return f.template go<ST, kModeModel, true, false, TX, TY>();
+      case kModeBornLin:
+        return f.template go<ST, kModeBornLin, true, true, TX, TY>();
+      case kModeBornAdj:
+        return f.template go<ST, kModeBornAdj, true, false, TX, TY>();
+      default: break;
+    }
+  }
+  switch (mode) {
+    case kModeSource: return f.template go<ST, kModeSource, true, false, TX, TY>();
+    case kModeForward:
+      return f.template go<ST, kModeForward, true, true, TX, TY>();
+    default:
+      if (pa && pb) return f.template go<ST, kModeAdjoint, true, true, TX, TY>();
+      if (pa) return f.template go<ST, kModeAdjoint, true, false, TX, TY>();
+      if (pb) return f.template go<ST, kModeAdjoint, false, true, TX, TY>();
+      return f.template go<ST, kModeAdjoint, false, false, TX, TY>();
+  }
+}
+
+template <int ST, class F>
+auto dispatch_cfg(int cfg, int mode, bool pa, bool pb, F f) {
+  switch (cfg) {
+    case 1: return dispatch<ST, 32, 16>(mode, pa, pb, f);
+    case 2: return dispatch<ST, 32, 32>(mode, pa, pb, f);
+    case 3: return dispatch<ST, 64, 8>(mode, pa, pb, f);
+    case 4: return dispatch<ST, 32, 8>(mode, pa, pb, f);
+    default: return dispatch<ST, 64, 16>(mode, pa, pb, f);
+  }
+}
+
+struct LaunchF {
+  const StepMaps &maps;
+  const StepParams &p;
+  cudaStream_t s;
+  template <int ST, int MODE, bool PA, bool PB, int TX, int TY>
+  cudaError_t go() const {
+    return launch_t<ST, MODE, PA, PB, TX, TY>(maps, p, s);
+  }
+};
+
+struct LaunchBatchedF {
+  const BatchShot *shots;
+  const int *block_start;
+  int nshots, total;
+  const StepVar &var;
+  cudaStream_t s;
+  template <int ST, int MODE, bool PA, bool PB, int TX, int TY>
+  cudaError_t go() const {
+    return launch_t_batched<ST, MODE, PA, PB, TX, TY>(shots, block_start,
+                                                      nshots, total, var, s);
+  }
+};
+
+struct SmemF {
+  template <int ST, int MODE, bool PA, bool PB, int TX, int TY>
+  size_t go() const {
+    return Layout<ST, MODE, PA, PB, TX, TY>::kSmem;
+  }
+};
+
+}  // namespace
+
+// Per-storage entry points, defined by the translation unit that owns the
+// storage type (born_step.cu, born_step_bf16.cu, born_step_f16.cu).
+#define BORN_DECLARE_STORAGE_ENTRY(NAME)                                     \
+  cudaError_t launch_step_##NAME(int mode, bool pa, bool pb, int cfg,        \
+                                 const StepMaps &maps, const StepParams &p,  \
+                                 cudaStream_t s);                            \
+  cudaError_t launch_step_batched_##NAME(                                    \
+      int mode, bool pa, bool pb, int cfg, const BatchShot *shots,           \
+      const int *block_start, int nshots, int total, const StepVar &var,     \
+      cudaStream_t s);                                                       \
+  size_t step_smem_##NAME(int cfg, int mode, bool pa, bool pb);
+
+BORN_DECLARE_STORAGE_ENTRY(f32)
+BORN_DECLARE_STORAGE_ENTRY(bf16)
+BORN_DECLARE_STORAGE_ENTRY(f16)
+
+#define BORN_DEFINE_STORAGE_ENTRY(ST, NAME)                                  \
+  cudaError_t launch_step_##NAME(int mode, bool pa, bool pb, int cfg,        \
+                                 const StepMaps &maps, const StepParams &p,  \
+                                 cudaStream_t s) {                           \
+    return dispatch_cfg<ST>(cfg, mode, pa, pb, LaunchF{maps, p, s});         \
+  }                                                                          \
+  cudaError_t launch_step_batched_##NAME(                                    \
+      int mode, bool pa, bool pb, int cfg, const BatchShot *shots,           \
+      const int *block_start, int nshots, int total, const StepVar &var,     \
+      cudaStream_t s) {                                                      \
+    return dispatch_cfg<ST>(                                                 \
+        cfg, mode, pa, pb,                                                   \
+        LaunchBatchedF{shots, block_start, nshots, total, var, s});          \
+  }                                                                          \
+  size_t step_smem_##NAME(int cfg, int mode, bool pa, bool pb) {             \
+    return dispatch_cfg<ST>(cfg, mode, pa, pb, SmemF{});                     \
+  }
+
+}  // namespace born

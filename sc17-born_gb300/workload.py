@@ -21,7 +21,8 @@ from __future__ import annotations
 
 import numpy as np
 
-SEEDS = dict(velocity=1001, reflectivity=1002, data=1004)
+SEEDS = dict(velocity=1001, reflectivity=1002, data=1004, jitter=1006,
+             aperture=1007)
 
 
 def ricker(nt: int, dt: float, f: float, t0: float = 0.064) -> np.ndarray:
@@ -85,6 +86,10 @@ CONFIGS = {
                rec=(64, 20.0), src_depth=20.0, rec_depth=10.0),
     "c2": dict(n=256, d=10.0, nbound=50, nt=2000, f=12.0, model=model_c2,
                rec=(128, 20.0), src_depth=20.0, rec_depth=10.0),
+    # 512^3 at 8 m: FD dt 0.5 ms against data dt 1 ms (jt = 2), so 1500
+    # data samples make 2999 FD steps
+    "c3": dict(n=512, d=8.0, nbound=50, nt=1500, f=20.0, model=model_c2,
+               rec=(128, 16.0), src_depth=16.0, rec_depth=8.0),
 }
 
 
@@ -147,3 +152,99 @@ def prepare_shot(born, name: str = "c2", nt: int | None = None,
 def interior_cells(shape) -> int:
     nz, ny, nx = shape
     return (nx - 8) * (ny - 8) * (nz - 8)
+
+
+# ---------------------------------------------------------------------------
+# c4: batched multi-shot RTM on a large model with uneven shot apertures
+
+def model_c4(nx=800, ny=800, nz=400, seed=SEEDS["velocity"]):
+    """Layered 1500..4500 m/s with a dipping interface and a Gaussian blob,
+    built by broadcasting (no full-size index grids)."""
+    rng = np.random.default_rng(seed)
+    z = np.arange(nz, dtype=np.float32)[:, None, None]
+    y = np.arange(ny, dtype=np.float32)[None, :, None]
+    x = np.arange(nx, dtype=np.float32)[None, None, :]
+    dip = np.float32(np.tan(np.deg2rad(rng.uniform(5, 15))))
+    v = np.empty((nz, ny, nx), np.float32)
+    v[...] = 1500.0 + 2500.0 * z / (nz - 1)
+    v += np.where(z > 0.55 * nz + dip * (x - nx / 2), np.float32(400.0),
+                  np.float32(0.0))
+    r2 = ((z - 0.6 * nz) ** 2 / (0.1 * nz) ** 2 +
+          ((y - 0.5 * ny) ** 2 + (x - 0.45 * nx) ** 2) / (0.08 * nx) ** 2)
+    blob = np.exp(-r2).astype(np.float32)
+    v = v * (1 - blob) + 4500.0 * blob
+    np.clip(v, 1500.0, 4500.0, out=v)
+    return v
+
+
+def c4_shots(nx=800, ny=800, d=10.0, gx=8, gy=6):
+    """Jittered 8 x 6 surface grid (+-25 % of the spacing) and per-shot
+    aperture sizes uniform in 192..320 (x, y) and 256..400 (z) cells,
+    rounded to 16."""
+    rj = np.random.default_rng(SEEDS["jitter"])
+    ra = np.random.default_rng(SEEDS["aperture"])
+    sx, sy = nx * d / gx, ny * d / gy
+    shots = []
+    for j in range(gy):
+        for i in range(gx):
+            x = (i + 0.5) * sx + rj.uniform(-0.25, 0.25) * sx
+            y = (j + 0.5) * sy + rj.uniform(-0.25, 0.25) * sy
+            ax = int(ra.integers(192, 321)) // 16 * 16
+            ay = int(ra.integers(192, 321)) // 16 * 16
+            az = int(ra.integers(256, 401)) // 16 * 16
+            shots.append((x, y, ax, ay, az))
+    return shots
+
+
+def prepare_batch_c4(born, nshots=48, nt=2500, nbound=40, f=15.0,
+                     model=None, device=0):
+    """Set-up shot handles for c4: each shot's compute grid is its aperture
+    centred on the source, velocities made on the device (random boundary
+    from counter-based draws), receivers every 25 m inside the aperture, data
+    traces seeded noise.  Returns (handles, common dict)."""
+    d = 10.0
+    vel = model_c4() if model is None else model
+    nz_m, ny_m, nx_m = vel.shape
+    vmax = float(vel.max())
+    dt_data = 0.001
+    dt, nt_fd = born.calc_stability(vmax, d, dt_data, nt)
+    jt = int(round(dt_data / dt))
+    table = born.sinc_table(jt, 8)
+    nt_big = nt + 8
+    wav = born.wavelet_deriv(ricker(nt, dt_data, f), dt_data)
+    rng = np.random.default_rng(SEEDS["data"])
+    handles = []
+    for k, (sx, sy, ax, ay, az) in enumerate(c4_shots()[:nshots]):
+        n1, n2, n3 = ax, ay, az
+        o = (sx - d * (n1 // 2), sy - d * (n2 // 2), -d * (nbound + 4))
+        h = born.Gb300Prop(device)
+        h.createSpace(d, d, d, 50.0, 0.0005, 0.0005, n1, n2, n3)
+        h.transferSincTableS(8, jt, table)
+        h.transferSincTableD(8, jt, table)
+        locs_s, src = born.source_geometry(sx, sy, 20.0, o, (d, d, d), n1, n2,
+                                           wav, nt_big)
+        h.transferSourceFunc(9, nt_big, locs_s, src)
+        # the model window the aperture covers (indices clamped as the
+        # reference's resampling does)
+        i0 = int(np.clip(np.floor(o[0] / d), 0, nx_m - 1))
+        j0 = int(np.clip(np.floor(o[1] / d), 0, ny_m - 1))
+        sub = vel[:, j0:min(ny_m, j0 + n2), i0:min(nx_m, i0 + n1)]
+        sub = np.ascontiguousarray(sub)
+        vo = (i0 * d, j0 * d, 0.0)
+        seed = int(locs_s[3] % 10000)
+        h.make_velocity(1, sub, vo, (d, d, d), vmax, seed,
+                        (nbound, nbound, nbound), dt, o, (d, d, d))
+        h.make_velocity(2, sub, vo, (d, d, d), vmax, seed, (0, 0, 0), dt, o,
+                        (d, d, d))
+        margin = (nbound + 4) * d
+        nrx = int((n1 * d - 2 * margin) // 25.0)
+        nry = int((n2 * d - 2 * margin) // 25.0)
+        locs_r = born.receiver_geometry(nrx, nry, o[0] + margin, 25.0,
+                                        o[1] + margin, 25.0, 10.0, o,
+                                        (d, d, d), n1, n2)
+        rec = np.zeros((nrx * nry, nt_big), np.float32)
+        rec[:, 4:4 + nt] = 1e-3 * rng.standard_normal((nrx * nry, nt),
+                                                      dtype=np.float32)
+        h.transferReceiverFunc(nrx, nry, nt_big, locs_r, rec)
+        handles.append(h)
+    return handles, dict(nt=nt_fd, jt=jt, nbound=nbound)
