@@ -31,6 +31,11 @@
 // plus the exact linearised Born pair (modes kModeBornLin / kModeBornAdj)
 // and plain nonlinear modelling (kModeModel), used for the dot-product and
 // finite-difference checks and for least-squares migration.
+//
+// The levels of the propagated fields may be stored as FP32 (the parity
+// path), BF16 or FP16 (Storage): 16-bit levels carry a power-of-two scale
+// each, chosen on the device from a bound on the level's magnitude, and are
+// decoded to FP32 as they are read; the arithmetic stays FP32.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>

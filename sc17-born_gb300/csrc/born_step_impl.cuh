@@ -849,18 +849,27 @@ template <int ST, int MODE, bool PA, bool PB, int TX, int TY>
 __global__ void __launch_bounds__(Tile<TX, TY, 4>::kThreads)
     step_kernel_batched(const BatchShot *shots, const int *block_start,
                         int nshots, const StepVar var) {
-  __shared__ StepParams sp;
-  __shared__ int s_shot, s_local;
+  __shared__ __align__(16) StepParams sp;
+  static_assert(sizeof(StepParams) % 4 == 0, "word-wise copy");
+  // every thread finds the shot (same addresses: broadcast loads) and the
+  // CTA copies the shot's parameters word by word
+  int lo = 0, hi = nshots - 1;  // last shot whose start <= blockIdx.x
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (block_start[mid] <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+  }
+  const int shot = lo, local = (int)blockIdx.x - block_start[lo];
+  {
+    const unsigned int *src =
+        reinterpret_cast<const unsigned int *>(&shots[shot].params);
+    unsigned int *dst = reinterpret_cast<unsigned int *>(&sp);
+    for (int i = threadIdx.x; i < (int)(sizeof(StepParams) / 4);
+         i += blockDim.x)
+      dst[i] = src[i];
+  }
+  __syncthreads();
   if (threadIdx.x == 0) {
-    int lo = 0, hi = nshots - 1;  // last shot whose start <= blockIdx.x
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) / 2;
-      if (block_start[mid] <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
-    }
-    s_shot = lo;
-    s_local = (int)blockIdx.x - block_start[lo];
-    const BatchShot &b = shots[lo];
-    sp = b.params;
+    const BatchShot &b = shots[shot];
     sp.a_out = b.a_out[var.parity];
     sp.b_out = b.b_out[var.parity];
     sp.pa.id = var.pa_id;
@@ -877,10 +886,10 @@ __global__ void __launch_bounds__(Tile<TX, TY, 4>::kThreads)
     sp.lb = var.lb;
   }
   __syncthreads();
-  const BatchShot &b = shots[s_shot];
+  const BatchShot &b = shots[shot];
   const int ntiles = sp.tiles_x * sp.tiles_y;
-  step_body<ST, MODE, PA, PB, TX, TY>(&b.maps[var.parity], sp,
-                                      s_local % ntiles, s_local / ntiles);
+  step_body<ST, MODE, PA, PB, TX, TY>(&b.maps[var.parity], sp, local % ntiles,
+                                      local / ntiles);
 }
 
 // ---------------------------------------------------------------------------
