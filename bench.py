@@ -17,6 +17,17 @@ the RTM adjoint (sourceProp + rtmAdjoint) of configuration c2 (256^3 model,
 ``--impl reference`` times the reference CPU implementation instead (the
 compiled reference where it exists on this machine, else the oracle port).
 Multi-GPU: shots are independent, so N ranks run N shots (weak scaling).
+
+Other configurations print their own line:
+  --config c3  one 624^3 shot (512^3 model at 8 m, jt = 2, nt = 2999) per
+               level storage (--storage f32,bf16,f16), 16-bit results
+               compared with the FP32 result of the same run
+  --config c4  48 shots of uneven aperture advanced together (one launch per
+               step, time loops as CUDA graphs) against the same shots one
+               after another (--storage for the level storage)
+  --config c5  least-squares RTM: --steps CG iterations over --shots shots
+               of the exact linearised pair (reduced model by default;
+               --model-n 384 gives the full 384 x 384 x 256)
 """
 from __future__ import annotations
 
@@ -630,19 +641,91 @@ def run_storage(args):
     return 0
 
 
+def run_lsrtm(args):
+    """c5: least-squares RTM, Claerbout CG (cgstep) with FP64 dots and step
+    lengths on the device, over the exact linearised Born pair of several
+    shots (checkpointed background in the adjoint).  Observed data come from
+    the same FP32 operator applied to a seeded sparse layered reflectivity;
+    reported: rr.rr per iteration, model error, time per iteration."""
+    import torch
+    born = package()
+    born.lib()
+    n1 = n2 = args.model_n or 128     # the full config: 384 x 384 x 256
+    n3 = max(32, (2 * n1) // 3)
+    d, nt_data, dt_data, f = 10.0, args.nt or 400, 0.001, 15.0
+    rng = np.random.default_rng(1005)
+    z = np.arange(n3, dtype=np.float32)[:, None, None]
+    x = np.arange(n1, dtype=np.float32)[None, None, :]
+    vel = 1500.0 + 2500.0 * z / (n3 - 1) + 0 * x
+    vel = np.where(z > 0.5 * n3 + 0.1 * (x - n1 / 2), vel + 300.0, vel)
+    vel = np.broadcast_to(vel, (n3, n2, n1)).astype(np.float32)
+    m_true = np.zeros((n3, n2, n1), np.float32)
+    for zl in rng.choice(np.arange(n3 // 4, n3 - 8), size=6, replace=False):
+        m_true[zl] = rng.choice([-1.0, 1.0]) * 1e-3  # sparse layered spikes
+    ns = int(round(np.sqrt(args.shots)))
+    sx = (np.arange(ns) + 0.5) * (n1 * d / ns)
+    shots = np.array([[a, b, 2 * d] for b in sx for a in sx], np.float32)
+    t = -1.2 / f + np.arange(nt_data) * dt_data
+    a = (np.pi * f * t) ** 2
+    wav = ((1 - 2 * a) * np.exp(-a)).astype(np.float32)
+    nr = max(8, n1 // 2)
+    t0 = time.perf_counter()
+    rd = d * (n1 - 2) / nr  # receivers spread over the model surface
+    op = born.BornOperator(vel, (0., 0., 0.), (d, d, d), shots, wav, dt_data,
+                           nt_data, dt_data, (nr, nr), (d, d), (rd, rd), d,
+                           40, exact=True, ckpt_interval=50)
+    setup_s = time.perf_counter() - t0
+    mt = torch.from_numpy(m_true).cuda()
+    d_obs = torch.zeros(op.data_shape, device="cuda")
+    op.forward(False, mt, d_obs)
+    m = torch.zeros(op.model_shape, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with Clocks(0) as clk:
+        res = op.cg(d_obs, m, args.steps)
+        torch.cuda.synchronize()
+    t_cg = time.perf_counter() - t0
+    mm = m.cpu().numpy()
+    err = float(np.linalg.norm(mm - m_true) / np.linalg.norm(m_true))
+    nc = [int(op.lib.born_compute_size(k, 40, 4)) for k in (n1, n2, n3)]
+    n_int = (nc[0] - 8) * (nc[1] - 8) * (nc[2] - 8)
+    # per CG iteration: one forward (background + scattered field) and one
+    # exact adjoint (background sweep, segment recomputation, adjoint field)
+    cu = 5.0 * n_int * op.nt_fd * len(shots)
+    line = {"metric": "CG iterations/s least-squares RTM (c5)",
+            "value": round(args.steps / t_cg, 4), "unit": "iterations/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": 0,
+            "ms_per_step": round(1e3 * t_cg / args.steps, 1),
+            "higher_is_better": True, "dtype": "f32 (FP64 dots and steps)",
+            "data": "synthetic (seeded layered velocity and sparse layered "
+                    "reflectivity; data = the FP32 operator applied to it)",
+            "config": {"workload": f"c5: {len(shots)} shots, model "
+                       f"{n1}x{n2}x{n3} at {d:.0f} m, nt_data={nt_data} "
+                       f"(FD nt={op.nt_fd}), exact linearised Born pair",
+                       "full_config": "384x384x256, nt=2000 (--model-n 384)"},
+            "rr_per_iteration": [float(r) for r in res],
+            "rr_reduction": float(res[-1] / res[0]),
+            "model_rel_error": err,
+            "field_updates_per_s_G": round(cu / (t_cg / args.steps) / 1e9, 2),
+            "setup_s": round(setup_s, 1), "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (c5: CG iterations; default 5, c5: 10)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--config", default="c2",
-                    choices=["c1", "c2", "c3", "c4"])
+                    choices=["c1", "c2", "c3", "c4", "c5"])
     ap.add_argument("--storage", default=None,
                     help="level storage: f32, bf16 or f16 (c3: a comma list,"
                          " default f32,bf16,f16; c4: one, default f32)")
-    ap.add_argument("--shots", type=int, default=48,
-                    help="c4: number of shots in the batch")
+    ap.add_argument("--shots", type=int, default=None,
+                    help="c4: shots in the batch (48); c5: shots (16)")
     ap.add_argument("--no-graph", action="store_true",
                     help="c4: launch step by step instead of CUDA graphs")
     ap.add_argument("--model-n", type=int, default=None,
@@ -656,6 +739,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 10 if args.config == "c5" else 5
+    if args.shots is None:
+        args.shots = 16 if args.config == "c5" else 48
     if args.warmup < 3 and args.impl == "gb300":
         print("note: warm-up raised to the minimum of 3", file=sys.stderr)
         args.warmup = 3
@@ -667,6 +754,8 @@ def main():
     if args.config == "c4":
         args.storage = args.storage or "f32"
         return run_batched(args)
+    if args.config == "c5":
+        return run_lsrtm(args)
     return run_gpu_arm(args)
 
 
