@@ -614,6 +614,11 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   const int ce = ly * TX + 4 * lx;                     // FP32 centre element
   float mx_a = 0.f, mx_b = 0.f;  // max |stored value| (16-bit storage)
 
+  // unrolling by 3 realigns the z window's registers every third plane
+  // instead of shifting it every plane (measured: source and forward steps
+  // 2-4 % faster, the two-field adjoint step 6 % slower)
+  constexpr int kUnroll = MODE == kModeAdjoint ? 1 : 3;
+#pragma unroll kUnroll
   for (int k = 0; k < K; ++k) {
     const int st = k % kZStages;
     const int j = k - 2 * kRadius;       // output index once k >= 8
