@@ -367,10 +367,16 @@ int tune_mode(born_handle *h, int mode) {
   if (!h->have_vel1 || !h->have_vel2) return BORN_OK;  // nothing to time yet
   float *timg = nullptr;
   CK(h, cudaMalloc(&timg, (size_t)h->n123 * 4));
-  CK(h, cudaMemsetAsync(timg, 0, (size_t)h->n123 * 4, h->stream));
-  cudaEvent_t e0, e1;
-  CK(h, cudaEventCreate(&e0));
-  CK(h, cudaEventCreate(&e1));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaMemsetAsync(timg, 0, (size_t)h->n123 * 4, h->stream) !=
+          cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess ||
+      cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    cudaStreamSynchronize(h->stream);
+    cudaFree(timg);
+    return fail(h, BORN_ECUDA, "autotuner setup failed");
+  }
   const int saved = h->tile_cfg;
   int best = -1;
   float best_ms = 0.f;

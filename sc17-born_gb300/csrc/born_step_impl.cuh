@@ -565,6 +565,14 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   if (tid < kNBound) s_bound[tid] = p.bound[tid];
   __syncthreads();
   if (abort_flag) return;  // uniform: read after the barrier
+  // The taper factor of a cell is B(min(ex, ey, ez)) with B(e) = bound[e]
+  // for e < 40 and 1 beyond: B does not decrease over the interior (e >= 0),
+  // so the factor is min(B(min(ex, ey)), B(ez)) exactly -- one value per
+  // x/y position here, one per plane below
+  float bxy[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+    bxy[j] = (exy[j] >= 0 && exy[j] < kNBound) ? s_bound[exy[j]] : 1.0f;
 
   const int K = (z1 - z0) + 2 * kRadius;  // z-window planes z0-4 .. z1+3
   const int J = z1 - z0;                  // output planes
@@ -689,11 +697,11 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
           sb = stencil4<BX>(reinterpret_cast<const float *>(box_b), brow,
                             bcol, qb, p.c, cb);
       }
+      const float bz = ez < kNBound ? s_bound[ez] : 1.0f;  // ez >= 0 here
       float bj[4];
 #pragma unroll
       for (int jj = 0; jj < 4; ++jj) {
-        const int e = min(exy[jj], ez);
-        const float b = (e >= 0 && e < kNBound) ? s_bound[e] : 1.0f;
+        const float b = fminf(bxy[jj], bz);
         bj[jj] = b;
         if (M::kBoxA) {
           float old = comp(oa, jj);

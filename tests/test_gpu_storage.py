@@ -126,3 +126,16 @@ def test_storage_rejects_fp32_only_paths(gpu, case):
                   nz)
     with pytest.raises(born.BornError):  # 16-bit rows need nx % 8 == 0
         q.set_storage("f16")
+
+
+def test_f16_odd_nt_and_jt2_against_fp64(gpu, po):
+    # jt = 2 (sinc interpolation) and odd nt (the final level copy of the
+    # source propagation and the last pending source injection of the
+    # adjoint act on 16-bit levels and their records)
+    c = cases.make_case(73, shape=(32, 36, 48), nt=121, jt=2,
+                        sinc=po.sinc_table)
+    want = po.run_case(po.PortProp64(), c)
+    img, tr = run_device(gpu, c, "f16")
+    e = (rel(img, want["image"]), rel(tr, want["traces"]))
+    print(f"f16 jt=2 nt=121: image rel L2 {e[0]:.3e}, traces {e[1]:.3e}")
+    assert max(e) <= 1e-2, e
