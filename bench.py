@@ -281,6 +281,7 @@ def run_gpu_arm(args):
         prop.set_tiling(args.tile, args.zseg)
     prop.createSpace(case["d"], case["d"], case["d"], 50.0, 0.0005, 0.0005,
                      nx, ny, nz)
+    prop.set_storage(args.storage or "f32")
     prop.transferSincTableS(8, jt, case["table_s"])
     prop.transferSincTableD(8, jt, case["table_d"])
     prop.transferSourceFunc(9, case["nt_big"], case["locs_s"], case["src"])
@@ -335,6 +336,29 @@ def run_gpu_arm(args):
     adj_ms = sum(e[2].elapsed_time(e[3]) for e in evs) / args.steps
     value = aggregate_rate(cells_per_step, args.steps, t_ms, world)
 
+    # the same loops with FP32 levels and fused multiply-add arithmetic
+    # (within 1.4e-6 relative L2 of the reference order in the tests)
+    fused = None
+    if (args.storage or "f32") == "f32" and not args.no_fused:
+        prop.set_storage("f32fma")
+        for _ in range(2):  # warm-up, including the tuner for this storage
+            device_step()
+        prop.synchronize()
+        fev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)]
+               for _ in range(2)]
+        for k in range(2):
+            device_step(fev[k])
+        prop.synchronize()
+        f_ms = [sum(e[i].elapsed_time(e[i + 1]) for e in fev) / 2
+                for i in range(3)]
+        fused = {"value": round(cells_per_step / (sum(f_ms) / 1e3) / 1e9, 3),
+                 "unit": "Gcell-updates/s", "steps": 2,
+                 "forward_ms": round(f_ms[0], 2), "source_ms": round(f_ms[1], 2),
+                 "adjoint_ms": round(f_ms[2], 2),
+                 "arith": "FP32 levels, fused multiply-add stencil and "
+                          "leapfrog (born_set_storage BORN_STORE_F32_FUSED)"}
+        prop.set_storage("f32")
+
     # roofline of the dominant kernel: the fused RTM adjoint step
     peak, peak_kind = measured_peak()
     adj_launch_ms = adj_ms / nt
@@ -370,18 +394,21 @@ def run_gpu_arm(args):
             "unit": "Gcell-updates/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(t_ms / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded, shapes of the config)",
+            "dtype": "f32" if (args.storage or "f32") == "f32" else
+                     "f32 arithmetic; levels " + args.storage,
+            "data": "synthetic (seeded, shapes of the config)",
             "config": {"workload": f"{args.config}: 3D Born forward + RTM "
                        f"adjoint, compute grid {nx}x{ny}x{nz}, nt={nt}, "
                        "random-boundary source reconstruction",
                        "grid": [nz, ny, nx], "nt": nt, "jt": jt,
                        "interior_cells": n_int,
+                       "storage": args.storage or "f32",
                        "l2": "inputs larger than L2 (7 x %.0f MB fields)" %
                              (nx * ny * nz * 4 / 1e6),
                        "parallelism": f"shots x{world} (one per GPU)"},
             "roofline": roofline, "phases": phases, "tile_cfg": tiles,
             "clocks": clk.summary(), "gpu_launches": launches,
-            "e2e": e2e, "cpu_baseline": cpu,
+            "e2e": e2e, "cpu_baseline": cpu, "fused_fma": fused,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -738,6 +765,8 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fused", action="store_true",
+                    help="c2: skip the extra fused multiply-add measurement")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 10 if args.config == "c5" else 5

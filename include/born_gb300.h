@@ -318,6 +318,11 @@ long long born_kernel_launches(const born_handle *h);
 #define BORN_STORE_F32 0
 #define BORN_STORE_BF16 1
 #define BORN_STORE_F16 2
+/* FP32 levels with the stencil and leapfrog formed by fused multiply-adds
+ * in the source, adjoint and forward loops: not bit-identical to the
+ * reference (within a relative L2 of 1e-5 of it), fewer instructions per
+ * cell.  The other loops keep the reference order. */
+#define BORN_STORE_F32_FUSED 3
 int born_set_storage(born_handle *h, int storage);
 int born_get_storage(const born_handle *h);
 /* Raw CUDA stream of the handle (cudaStream_t), for event timing. */

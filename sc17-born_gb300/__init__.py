@@ -245,11 +245,13 @@ class Handle:
     def autotune(self, enable: bool = True):
         self.check(self.lib.born_autotune(self.h, int(enable)))
 
-    STORAGE = {"f32": 0, "bf16": 1, "f16": 2}
+    STORAGE = {"f32": 0, "bf16": 1, "f16": 2, "f32fma": 3}
 
     def set_storage(self, storage: str = "f32"):
-        """Storage of the wavefield levels: "f32", "bf16" or "f16" (16-bit
-        values with a power-of-two scale per level, FP32 arithmetic)."""
+        """Storage of the wavefield levels: "f32" (reference operation
+        order), "f32fma" (FP32 levels, fused multiply-add stencil), "bf16" or
+        "f16" (16-bit values with a power-of-two scale per level, FP32
+        arithmetic)."""
         self.check(self.lib.born_set_storage(self.h, self.STORAGE[storage]))
 
     @property

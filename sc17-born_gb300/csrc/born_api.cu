@@ -267,7 +267,8 @@ void pick_tiling(born_handle *h, int mode, bool pa, bool pb, int *cfg,
   }
   int sms = 148;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-  const size_t smem = born::step_smem_bytes(h->storage, c, mode, pa, pb);
+  const size_t smem =
+      born::step_smem_bytes(h->storage_for(mode), c, mode, pa, pb);
   int per_sm = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
   per_sm = std::min(per_sm, 2048 / ((tx / 4) * ty));
   const long long target = 2ll * sms * per_sm;
@@ -348,7 +349,8 @@ int launch(born_handle *h, int mode, bool pa, bool pb, const void *a_cur,
                  cfg, 1, es, &maps.cm[sl]);
   }
   if (rc) return rc;
-  CK(h, born::launch_step(h->storage, mode, pa, pb, cfg, maps, p, h->stream));
+  CK(h, born::launch_step(h->storage_for(mode), mode, pa, pb, cfg, maps, p,
+                          h->stream));
   h->launches++;
   return BORN_OK;
 }
@@ -381,7 +383,7 @@ int tune_mode(born_handle *h, int mode) {
   int best = -1;
   float best_ms = 0.f;
   int rc = BORN_OK;
-  const bool lp = h->storage != born::kStoreF32;
+  const bool lp = h->lp();
   if (lp) {
     const void *reset[] = {h->f0, h->f1, h->r0, h->r1};
     rc = born_lp_prologue(h, h->stream, reset, 4);
@@ -526,7 +528,7 @@ void born_level_written(born_handle *h, const void *buf) {
 
 int born_lp_prologue(born_handle *h, cudaStream_t s, const void *const *reset,
                      int nreset) {
-  if (h->storage == born::kStoreF32) return BORN_OK;
+  if (!h->lp()) return BORN_OK;
   unsigned int *st = h->stat_dev;
   CK(h, cudaMemsetAsync(st, 0, kNumStats * sizeof(unsigned int), s));
   const float *arr[3] = {h->vel1, h->vel2, h->refl};
@@ -557,7 +559,7 @@ int born_copy_level(born_handle *h, void *dst, const void *src,
   CK(h, cudaMemcpyAsync(dst, src, h->level_bytes(), cudaMemcpyDeviceToDevice,
                         s));
   const int d = born_level_id(h, dst), c = born_level_id(h, src);
-  if (h->storage != born::kStoreF32 && d >= 0 && c >= 0) {
+  if (h->lp() && d >= 0 && c >= 0) {
     CK(h, born::launch_level_copy(h->lv_dev, 2 * d + ((h->wr[d] + 1) & 1),
                                   2 * c + (h->wr[c] & 1), tag, s));
     h->launches++;
@@ -748,7 +750,7 @@ int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
   if (nt < 0 || jts < 1) return fail(h, BORN_EINVAL, "nt < 0 or jts < 1");
   if (!h->have_vel1) return fail(h, BORN_ESTATE, "vel1 not transferred");
   if (h->jt_s < 1) return fail(h, BORN_ESTATE, "source sinc table missing");
-  if ((p0_out || p1_out) && h->storage != born::kStoreF32)
+  if ((p0_out || p1_out) && h->lp())
     return fail(h, BORN_ESTATE, "host copies of the levels need FP32 storage");
   h->jt = jts;
   rc = ensure_tuned(h, kModeSource);
@@ -941,7 +943,7 @@ int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out) {
 int born_model(born_handle *h, int jt, int nt, float *traces_out) {
   int rc = check_ready(h);
   if (rc) return rc;
-  if (h->storage != born::kStoreF32)
+  if (h->lp())
     return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
   if (nt < 0 || jt < 1) return fail(h, BORN_EINVAL, "nt < 0 or jt < 1");
   if (!h->have_vel2) return fail(h, BORN_ESTATE, "vel2 not transferred");
@@ -980,7 +982,7 @@ int born_model(born_handle *h, int jt, int nt, float *traces_out) {
 int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
   int rc = check_ready(h);
   if (rc) return rc;
-  if (h->storage != born::kStoreF32)
+  if (h->lp())
     return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
   if (nt < 0 || jt < 1) return fail(h, BORN_EINVAL, "nt < 0 or jt < 1");
   if (!h->have_vel2 || !h->have_refl)
@@ -1037,7 +1039,7 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
                      float *model_out) {
   int rc = check_ready(h);
   if (rc) return rc;
-  if (h->storage != born::kStoreF32)
+  if (h->lp())
     return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
   if (nt < 1 || jt < 1 || interval < 1)
     return fail(h, BORN_EINVAL, "nt, jt and interval must be >= 1");
@@ -1148,7 +1150,7 @@ int born_get_traces(born_handle *h, float *out) {
 int born_get_source_levels(born_handle *h, float *p0_out, float *p1_out) {
   int rc = check_ready(h);
   if (rc) return rc;
-  if (h->storage != born::kStoreF32)
+  if (h->lp())
     return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
   const size_t bytes = (size_t)h->n123 * 4;
   if (p0_out) CK(h, cudaMemcpyAsync(p0_out, h->s0, bytes, cudaMemcpyDeviceToHost, h->stream));
@@ -1159,7 +1161,7 @@ int born_get_source_levels(born_handle *h, float *p0_out, float *p1_out) {
 int born_set_source_levels(born_handle *h, const float *p0, const float *p1) {
   int rc = check_ready(h);
   if (rc) return rc;
-  if (h->storage != born::kStoreF32)
+  if (h->lp())
     return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
   if (!p0 || !p1) return fail(h, BORN_EINVAL, "null source level");
   const size_t bytes = (size_t)h->n123 * 4;
@@ -1199,7 +1201,7 @@ int born_autotune(born_handle *h, int enable) {
                        born::kModeModel, born::kModeBornLin,
                        born::kModeBornAdj};
   for (int m : modes) {
-    if (h->storage != born::kStoreF32 && m > kModeAdjoint) continue;
+    if (h->lp() && m > kModeAdjoint) continue;
     rc = tune_mode(h, m);
     if (rc) return rc;
   }
@@ -1228,9 +1230,9 @@ int born_set_storage(born_handle *h, int storage) {
   int rc = check_ready(h);
   if (rc) return rc;
   if (storage != BORN_STORE_F32 && storage != BORN_STORE_BF16 &&
-      storage != BORN_STORE_F16)
+      storage != BORN_STORE_F16 && storage != BORN_STORE_F32_FUSED)
     return fail(h, BORN_EINVAL, "unknown storage %d", storage);
-  if (storage != BORN_STORE_F32 && h->n1 % 8 != 0)
+  if (born::storage_16bit(storage) && h->n1 % 8 != 0)
     return fail(h, BORN_EINVAL,
                 "16-bit storage needs nx %% 8 == 0 (rows of 16-byte multiples)");
   CK(h, cudaStreamSynchronize(h->stream));

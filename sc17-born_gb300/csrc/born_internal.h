@@ -80,10 +80,11 @@ struct born_handle {
   // autotuner: best tile configuration per storage and step mode (-1: not
   // tuned yet)
   bool autotune = true;
-  int tuned_cfg[3][6] = {{-1, -1, -1, -1, -1, -1},
+  int tuned_cfg[4][6] = {{-1, -1, -1, -1, -1, -1},
+                         {-1, -1, -1, -1, -1, -1},
                          {-1, -1, -1, -1, -1, -1},
                          {-1, -1, -1, -1, -1, -1}};
-  float tuned_ms[3][6] = {};
+  float tuned_ms[4][6] = {};
   // wavefield level storage (born::Storage) and, for 16-bit storage, the
   // level records [kNumLevelBufs][2 slots][2 words], the number of writes of
   // each level buffer since its last reset (its record slot is the parity)
@@ -93,9 +94,18 @@ struct born_handle {
   unsigned int *stat_dev = nullptr;
   int wr[kNumLevelBufs] = {};
   size_t level_bytes() const {
-    return (size_t)n123 * (storage == born::kStoreF32 ? 4 : 2);
+    return (size_t)n123 * born::storage_esize(storage);
   }
-  int level_esize() const { return storage == born::kStoreF32 ? 4 : 2; }
+  int level_esize() const { return born::storage_esize(storage); }
+  bool lp() const { return born::storage_16bit(storage); }
+  // storage a step mode runs with: the fused FP32 arithmetic covers the
+  // source, forward and adjoint steps; the other modes keep the reference
+  // order
+  int storage_for(int mode) const {
+    return (storage == born::kStoreF32Fused && mode > born::kModeAdjoint)
+               ? born::kStoreF32
+               : storage;
+  }
   long long launches = 0;
   int ntblock = 0;
   // TMA descriptors by (buffer, tile config * 2 + kind); kind 0 = halo box,

@@ -93,6 +93,7 @@ size_t step_smem_bytes(int storage, int cfg, int mode, bool pa, bool pb) {
   switch (storage) {
     case kStoreBF16: return step_smem_bf16(cfg, mode, pa, pb);
     case kStoreF16: return step_smem_f16(cfg, mode, pa, pb);
+    case kStoreF32Fused: return step_smem_f32fused(cfg, mode, pa, pb);
     default: return step_smem_f32(cfg, mode, pa, pb);
   }
 }
@@ -110,6 +111,9 @@ cudaError_t launch_step(int storage, int mode, bool pa, bool pb, int cfg,
     case kStoreF16:
       if (!lp_mode(mode)) return cudaErrorInvalidValue;
       return launch_step_f16(mode, pa, pb, cfg, maps, p, s);
+    case kStoreF32Fused:
+      if (!lp_mode(mode)) return cudaErrorInvalidValue;
+      return launch_step_f32fused(mode, pa, pb, cfg, maps, p, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -134,6 +138,9 @@ cudaError_t launch_step_batched(int storage, int mode, bool pa, bool pb,
       return launch_step_batched_f16(mode, pa, pb, cfg, shots,
                                                block_start, nshots, total, var,
                                                s);
+    case kStoreF32Fused:
+      return launch_step_batched_f32fused(mode, pa, pb, cfg, shots,
+                                          block_start, nshots, total, var, s);
     default: return cudaErrorInvalidValue;
   }
 }
@@ -150,7 +157,7 @@ cudaError_t launch_point_inject(const PointSet &ps, int npts, void *field,
       point_inject_kernel<kStoreF16><<<1, 32, 0, stream>>>(ps, npts, field, lv,
                                                            rec);
       break;
-    default:
+    default:  // FP32 levels, whatever the arithmetic
       point_inject_kernel<kStoreF32><<<1, 32, 0, stream>>>(ps, npts, field, lv,
                                                            rec);
   }

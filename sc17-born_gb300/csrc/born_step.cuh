@@ -78,10 +78,18 @@ struct PointSet {
   int mult;
 };
 
-// Storage of the propagated wavefield levels.  Velocities, image and
-// reflectivity stay FP32; with 16-bit storage the stencil still accumulates
-// in FP32 and every stored level carries its own power-of-two scale.
-enum Storage : int { kStoreF32 = 0, kStoreBF16 = 1, kStoreF16 = 2 };
+// Storage of the propagated wavefield levels (and the arithmetic that goes
+// with it).  Velocities, image and reflectivity stay FP32.  kStoreF32 keeps
+// the reference's operation order (bit-identical results); kStoreF32Fused
+// keeps FP32 levels but forms the stencil and leapfrog with fused
+// multiply-adds; with 16-bit storage the stencil still accumulates in FP32
+// (fused) and every stored level carries its own power-of-two scale.
+enum Storage : int { kStoreF32 = 0, kStoreBF16 = 1, kStoreF16 = 2,
+                     kStoreF32Fused = 3 };
+inline bool storage_16bit(int st) {
+  return st == kStoreBF16 || st == kStoreF16;
+}
+inline int storage_esize(int st) { return storage_16bit(st) ? 2 : 4; }
 
 // Per-level scale records (16-bit storage).  Each level buffer has two
 // record slots, used alternately by its successive writes, so that a step

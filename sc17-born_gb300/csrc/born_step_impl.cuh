@@ -103,14 +103,16 @@ __device__ __forceinline__ float absmax4(const float4 &v, float m) {
 
 template <int ST>
 struct Store {
-  static constexpr int kBytes = ST == kStoreF32 ? 4 : 2;
-  static constexpr bool kLow = ST != kStoreF32;
+  static constexpr bool kLow = ST == kStoreBF16 || ST == kStoreF16;
+  static constexpr int kBytes = kLow ? 2 : 4;
+  // fused multiply-add arithmetic (every storage but the reference order)
+  static constexpr bool kFused = ST != kStoreF32;
 };
 
 // Four consecutive values starting at element `e` of a shared tile.
 template <int ST>
 __device__ __forceinline__ float4 ld4(const unsigned char *base, int e) {
-  if constexpr (ST == kStoreF32) {
+  if constexpr (!Store<ST>::kLow) {
     return *reinterpret_cast<const float4 *>(base + 4 * e);
   } else {
     const uint2 u = *reinterpret_cast<const uint2 *>(base + 2 * e);
@@ -137,7 +139,7 @@ __device__ __forceinline__ float clamp_f16(float x) {
 template <int ST>
 __device__ __forceinline__ void st4_level(void *base, long long idx,
                                           const float4 &v) {
-  if constexpr (ST == kStoreF32) {
+  if constexpr (!Store<ST>::kLow) {
     *reinterpret_cast<float4 *>(static_cast<float *>(base) + idx) = v;
   } else {
     uint2 u;
@@ -158,7 +160,7 @@ __device__ __forceinline__ void st4_level(void *base, long long idx,
 
 template <int ST>
 __device__ __forceinline__ float ld1_level(const void *base, long long i) {
-  if constexpr (ST == kStoreF32) {
+  if constexpr (!Store<ST>::kLow) {
     return static_cast<const float *>(base)[i];
   } else if constexpr (ST == kStoreBF16) {
     const unsigned short b = static_cast<const unsigned short *>(base)[i];
@@ -170,7 +172,7 @@ __device__ __forceinline__ float ld1_level(const void *base, long long i) {
 
 template <int ST>
 __device__ __forceinline__ void st1_level(void *base, long long i, float v) {
-  if constexpr (ST == kStoreF32) {
+  if constexpr (!Store<ST>::kLow) {
     static_cast<float *>(base)[i] = v;
   } else if constexpr (ST == kStoreBF16) {
     static_cast<__nv_bfloat16 *>(base)[i] = __float2bfloat16_rn(v);
@@ -334,9 +336,10 @@ __device__ __forceinline__ float4 stencil4(const float *box, int brow,
   return make_float4(s[0], s[1], s[2], s[3]);
 }
 
-// The same sums over 16-bit stored values (raw units: the caller applies the
-// level's scale), with fused multiply-adds: the reduced-precision path is
-// judged by its error against FP64, not by bit equality.
+// The same sums with fused multiply-adds, over the stored values of any
+// storage (16-bit values in raw units: the caller applies the level's
+// scale).  Used by every storage but the reference-order FP32 one: these
+// paths are judged by their error, not by bit equality.
 template <int BX, int ST>
 __device__ __forceinline__ float4 stencil4_lp(const unsigned char *box,
                                               int brow, int bcol,
@@ -483,6 +486,7 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   using T = Tile<TX, TY, Store<ST>::kBytes>;
   using LY = Layout<ST, MODE, PA, PB, TX, TY>;
   constexpr bool LP = Store<ST>::kLow;
+  constexpr bool FUSED = Store<ST>::kFused;
   constexpr int NF = M::kNF;
   constexpr int BX = T::kBX;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -678,16 +682,20 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
         inject_row(p.pb, n1, n2, zo, gy, gx, ob);
 
       float4 na = oa, nb = ob, ga = zero4, sb = zero4, ca = zero4, cb = zero4;
-      if constexpr (LP) {
+      if constexpr (FUSED) {
         if (M::kBoxA) {
-          ga = scale4(stencil4_lp<BX, ST>(box_a, brow, bcol, qa, p.c, ca),
-                      s_sc.cur_a);
-          ca = scale4(ca, s_sc.cur_a);
+          ga = stencil4_lp<BX, ST>(box_a, brow, bcol, qa, p.c, ca);
+          if constexpr (LP) {
+            ga = scale4(ga, s_sc.cur_a);
+            ca = scale4(ca, s_sc.cur_a);
+          }
         }
         if (M::kBoxB) {
-          sb = scale4(stencil4_lp<BX, ST>(box_b, brow, bcol, qb, p.c, cb),
-                      s_sc.cur_b);
-          cb = scale4(cb, s_sc.cur_b);
+          sb = stencil4_lp<BX, ST>(box_b, brow, bcol, qb, p.c, cb);
+          if constexpr (LP) {
+            sb = scale4(sb, s_sc.cur_b);
+            cb = scale4(cb, s_sc.cur_b);
+          }
         }
       } else {
         if (M::kBoxA)
@@ -706,8 +714,8 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
         if (M::kBoxA) {
           float old = comp(oa, jj);
           if (M::kDampA) old = __fmul_rn(old, b);
-          float v = LP ? fmaf(comp(va, jj), comp(ga, jj),
-                              comp(ca, jj) + comp(ca, jj) - old)
+          float v = FUSED ? fmaf(comp(va, jj), comp(ga, jj),
+                                 comp(ca, jj) + comp(ca, jj) - old)
                        : leapfrog(comp(va, jj), comp(ga, jj), comp(ca, jj),
                                   old);
           // the adjoint of the linearised step injects its data before the
@@ -721,8 +729,8 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
         if (M::kBoxB) {
           float old = comp(ob, jj);
           if (M::kDampB) old = __fmul_rn(old, b);
-          float v = LP ? fmaf(comp(vb, jj), comp(sb, jj),
-                              comp(cb, jj) + comp(cb, jj) - old)
+          float v = FUSED ? fmaf(comp(vb, jj), comp(sb, jj),
+                                 comp(cb, jj) + comp(cb, jj) - old)
                        : leapfrog(comp(vb, jj), comp(sb, jj), comp(cb, jj),
                                   old);
           // linearised Born: scattering source m (A s) inside the taper
@@ -1024,7 +1032,8 @@ struct SmemF {
 }  // namespace
 
 // Per-storage entry points, defined by the translation unit that owns the
-// storage type (born_step.cu, born_step_bf16.cu, born_step_f16.cu).
+// storage type (born_step.cu, born_step_bf16.cu, born_step_f16.cu,
+// born_step_f32fused.cu).
 #define BORN_DECLARE_STORAGE_ENTRY(NAME)                                     \
   cudaError_t launch_step_##NAME(int mode, bool pa, bool pb, int cfg,        \
                                  const StepMaps &maps, const StepParams &p,  \
@@ -1038,6 +1047,7 @@ struct SmemF {
 BORN_DECLARE_STORAGE_ENTRY(f32)
 BORN_DECLARE_STORAGE_ENTRY(bf16)
 BORN_DECLARE_STORAGE_ENTRY(f16)
+BORN_DECLARE_STORAGE_ENTRY(f32fused)
 
 #define BORN_DEFINE_STORAGE_ENTRY(ST, NAME)                                  \
   cudaError_t launch_step_##NAME(int mode, bool pa, bool pb, int cfg,        \

@@ -139,3 +139,22 @@ def test_f16_odd_nt_and_jt2_against_fp64(gpu, po):
     e = (rel(img, want["image"]), rel(tr, want["traces"]))
     print(f"f16 jt=2 nt=121: image rel L2 {e[0]:.3e}, traces {e[1]:.3e}")
     assert max(e) <= 1e-2, e
+
+
+@pytest.mark.parametrize("seed,shape,nt,jt,dup", [
+    (81, (40, 44, 56), 120, 1, 0), (82, (36, 30, 40), 61, 2, 3)])
+def test_fused_fp32_within_parity_bound(gpu, po, seed, shape, nt, jt, dup):
+    # FP32 levels with fused multiply-adds: not bit-identical to the
+    # reference order, but within the 1e-5 relative L2 bound of plain FP32
+    c = cases.make_case(seed, shape=shape, nt=nt, jt=jt, dup_receivers=dup,
+                        sinc=po.sinc_table)
+    nz, ny, nx = shape
+    prop = gpu.Gb300Prop()
+    prop.createSpace(c["d"], c["d"], c["d"], 50, .0005, .0005, nx, ny, nz)
+    prop.set_storage("f32fma")
+    got = po.run_case(prop, c)
+    want = po.run_case(po.PortProp(), c)
+    for k, v in want.items():
+        e = rel(got[k], v)
+        print(f"f32fma {k}: rel L2 {e:.2e}")
+        assert e <= 1e-5, (k, e)
