@@ -5,7 +5,7 @@
 // three time loops.  The loops mirror the reference CPU propagator's pointer
 // rotation step for step (base/cpu_prop.cc:22-129) so that every kernel sees
 // the same levels the reference would; the arithmetic itself is in
-// born_step.cu.
+// born_step_impl.cuh.
 #include <cuda.h>
 #include <cuda_runtime.h>
 

@@ -33,9 +33,10 @@
 // finite-difference checks and for least-squares migration.
 //
 // The levels of the propagated fields may be stored as FP32 (the parity
-// path), BF16 or FP16 (Storage): 16-bit levels carry a power-of-two scale
-// each, chosen on the device from a bound on the level's magnitude, and are
-// decoded to FP32 as they are read; the arithmetic stays FP32.
+// path, reference operation order; or with fused multiply-adds), BF16 or
+// FP16 (Storage): 16-bit levels carry a power-of-two scale each, chosen on
+// the device from a bound on the level's magnitude, and are decoded to FP32
+// as they are read; the arithmetic stays FP32.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -173,8 +174,9 @@ cudaError_t launch_step_batched(int storage, int mode, bool prop_a,
                                 const StepVar &var, cudaStream_t stream);
 
 // Host-side launch entry (defined in born_step.cu).  prop_a / prop_b say
-// which fields are propagated this step (adjoint first/last steps).  16-bit
-// storage supports the source, forward and adjoint modes.
+// which fields are propagated this step (adjoint first/last steps).  The
+// 16-bit and fused FP32 storages support the source, forward and adjoint
+// modes.
 cudaError_t launch_step(int storage, int mode, bool prop_a, bool prop_b,
                         int tile_cfg, const StepMaps &maps,
                         const StepParams &p, cudaStream_t stream);

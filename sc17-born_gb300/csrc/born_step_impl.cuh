@@ -1,7 +1,8 @@
 // Templated body of the fused time-step kernels (design in born_step.cuh).
-// Included by born_step.cu (FP32 storage), born_step_bf16.cu and
-// born_step_f16.cu so that the three families compile in parallel; each
-// includer instantiates its storage types with BORN_DEFINE_STORAGE_ENTRY.
+// Included by born_step.cu (FP32 storage, reference order),
+// born_step_bf16.cu, born_step_f16.cu and born_step_f32fused.cu so that the
+// storage families compile in parallel; each includer instantiates its
+// storage type with BORN_DEFINE_STORAGE_ENTRY.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
