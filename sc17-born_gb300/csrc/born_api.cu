@@ -358,8 +358,8 @@ int launch(born_handle *h, int mode, bool pa, bool pb, const void *a_cur,
 int check_device_error(born_handle *h);
 
 // Autotuner: times every tile configuration of one step mode on the
-// current grid (one warm-up and three timed launches, CUDA events on the
-// handle's stream) and keeps the fastest, per storage type.  It runs on the
+// current grid (two sweeps of one warm-up and four timed launches, CUDA
+// events on the handle's stream) and keeps the fastest, per storage type.  It runs on the
 // scratch levels f0/f1/r0/r1 and a temporary image with every point set
 // inactive, so it never touches the source levels kept for rtm_adjoint nor
 // an image a caller has yet to read, and clears the levels it used.
@@ -388,7 +388,13 @@ int tune_mode(born_handle *h, int mode) {
     const void *reset[] = {h->f0, h->f1, h->r0, h->r1};
     rc = born_lp_prologue(h, h->stream, reset, 4);
   }
-  for (int cfg = 0; cfg < born::tile_cfg_count() && !rc; ++cfg) {
+  // two interleaved sweeps over the tiles, one warm-up and four timed
+  // launches each, best time per tile: a single short timing is noisy
+  // enough to pick a tile 5-7 % slower than the best
+  const int ncfg = born::tile_cfg_count();
+  std::vector<float> cfg_ms(ncfg, -1.f);
+  for (int sweep = 0; sweep < 2 * ncfg && !rc; ++sweep) {
+    const int cfg = sweep % ncfg;
     h->tile_cfg = cfg;
     StepParams p;
     base_params(h, p);
@@ -403,7 +409,7 @@ int tune_mode(born_handle *h, int mode) {
     }
     const void *cen[born::kNumCentre] = {h->f1, h->r1, h->vel2, h->vel1,
                                          mode == kModeForward ? h->refl : timg};
-    for (int it = 0; it < 4 && !rc; ++it) {
+    for (int it = 0; it < 5 && !rc; ++it) {
       if (it == 1) cudaEventRecord(e0, h->stream);
       rc = launch(h, mode, true, pb, h->f0, h->r0, cen, p);
     }
@@ -411,11 +417,14 @@ int tune_mode(born_handle *h, int mode) {
     cudaEventSynchronize(e1);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    if (!rc && (best < 0 || ms < best_ms)) {
-      best = cfg;
-      best_ms = ms;
-    }
+    ms /= 4.f;
+    if (!rc && (cfg_ms[cfg] < 0.f || ms < cfg_ms[cfg])) cfg_ms[cfg] = ms;
   }
+  for (int cfg = 0; cfg < ncfg; ++cfg)
+    if (cfg_ms[cfg] >= 0.f && (best < 0 || cfg_ms[cfg] < best_ms)) {
+      best = cfg;
+      best_ms = cfg_ms[cfg];
+    }
   h->tile_cfg = saved;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -423,7 +432,7 @@ int tune_mode(born_handle *h, int mode) {
   cudaFree(timg);
   if (rc) return rc;
   h->tuned_cfg[h->storage][mode] = best;
-  h->tuned_ms[h->storage][mode] = best_ms / 3.f;
+  h->tuned_ms[h->storage][mode] = best_ms;
   const size_t bytes = h->level_bytes();
   float *scratch[] = {h->f0, h->f1, h->r0, h->r1};
   for (float *b : scratch) CK(h, cudaMemsetAsync(b, 0, bytes, h->stream));

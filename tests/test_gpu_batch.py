@@ -38,7 +38,7 @@ def single(p, c):
     return img, p.get_traces(c["rec_in"])
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16"])
+@pytest.mark.parametrize("storage", ["f32", "f16", "f32fma"])
 @pytest.mark.parametrize("graph", [False, True])
 @pytest.mark.parametrize("jt", [1, 2])
 def test_batch_matches_single_shots(born, po, graph, jt, storage):
