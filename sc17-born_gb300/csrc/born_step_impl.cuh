@@ -7,6 +7,8 @@
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
+#include <atomic>
+
 #include "born_step.cuh"
 
 namespace born {
@@ -924,19 +926,32 @@ constexpr TileCfg kTileCfgs[] = {{64, 16}, {32, 16}, {32, 32}, {64, 8},
                                  {32, 8}};
 constexpr int kNumTileCfgs = sizeof(kTileCfgs) / sizeof(kTileCfgs[0]);
 
+// The dynamic shared-memory limit of a kernel is an attribute of the
+// current device: set it once per device (bit d of `done`; devices beyond
+// 63 set it on every launch).
+template <class K>
+cudaError_t configure_smem(K kern, size_t smem,
+                           std::atomic<unsigned long long> &done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = dev < 64 ? (1ull << dev) : 0ull;
+  if (bit && (done.load(std::memory_order_relaxed) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem);
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_relaxed);
+  return e;
+}
+
 template <int ST, int MODE, bool PA, bool PB, int TX, int TY>
 cudaError_t launch_t(const StepMaps &maps, const StepParams &p,
                      cudaStream_t stream) {
   using T = Tile<TX, TY, 4>;
   const size_t smem = Layout<ST, MODE, PA, PB, TX, TY>::kSmem;
   auto kern = step_kernel<ST, MODE, PA, PB, TX, TY>;
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(
-        kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};
+  cudaError_t e = configure_smem(kern, smem, configured);
+  if (e != cudaSuccess) return e;
   const int nseg = (p.n3 - 2 * kRadius + p.zseg - 1) / p.zseg;
   dim3 grid(p.tiles_x * p.tiles_y, nseg);
   kern<<<grid, T::kThreads, smem, stream>>>(maps, p);
@@ -950,13 +965,9 @@ cudaError_t launch_t_batched(const BatchShot *shots, const int *block_start,
   using T = Tile<TX, TY, 4>;
   const size_t smem = Layout<ST, MODE, PA, PB, TX, TY>::kSmem;
   auto kern = step_kernel_batched<ST, MODE, PA, PB, TX, TY>;
-  static bool configured = false;
-  if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(
-        kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    configured = true;
-  }
+  static std::atomic<unsigned long long> configured{0};
+  cudaError_t e = configure_smem(kern, smem, configured);
+  if (e != cudaSuccess) return e;
   if (total == 0) return cudaSuccess;  // configuration only
   kern<<<total, T::kThreads, smem, stream>>>(shots, block_start, nshots, var);
   return cudaGetLastError();
