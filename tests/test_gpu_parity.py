@@ -47,7 +47,7 @@ def test_gpu_matches_reference_fixture(gpu, po, path):
     check(got, out)
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2, 3])
+@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
 def test_gpu_matches_oracle_all_tile_configs(gpu, po, cfg):
     c = cases.make_case(31 + cfg, shape=(40, 44, 56), nt=60, jt=1,
                         sinc=po.sinc_table)
@@ -133,3 +133,33 @@ def test_invalid_points_rejected(gpu):
                                 np.zeros(16, np.float32))
     with pytest.raises(gpu.BornError):
         prop.rtm_adjoint_device(1, 10)  # no source levels yet
+
+
+def test_call_sequence_errors_are_status_codes(gpu):
+    # out-of-order calls and bad arguments return BORN_E* codes and leave the
+    # handle usable (the reference exits the process instead)
+    EINVAL, ESTATE = -1, -4
+    prop = gpu.Gb300Prop()
+    L, h = prop.lib, prop.h
+    assert L.born_source_prop(h, 1, 10, None, None) == ESTATE  # no grid
+    assert L.born_create_space(h, 10., 10., 10., 50., .0005, .0005,
+                               30, 24, 20) == EINVAL          # nx % 4 != 0
+    assert L.born_create_space(h, 10., 10., 10., 50., .0005, .0005,
+                               32, 8, 20) == EINVAL           # n < 9
+    prop.createSpace(10., 10., 10., 50, .0005, .0005, 32, 24, 20)
+    assert L.born_source_prop(h, 1, 10, None, None) == ESTATE  # no vel1
+    assert L.born_rtm_adjoint(h, 1, 10, 1, None) == ESTATE     # no velocities
+    assert L.born_rtm_forward(h, 1, 10, None) == ESTATE        # no vel2/refl
+    assert L.born_source_prop(h, 0, 10, None, None) == EINVAL  # jts < 1
+    assert L.born_set_tiling(h, 99, 0) == EINVAL
+    assert L.born_set_storage(h, 7) == EINVAL
+    assert L.born_error_string(h)  # the last failure's message is kept
+    # the handle still works after the errors
+    vel = np.full((20, 24, 32), 0.1, np.float32)
+    prop.transferVelFunc1(32, 24, 20, vel)
+    prop.transferVelFunc2(32, 24, 20, vel)
+    prop.transferSincTableS(8, 1, np.ones(8, np.float32) / 8)
+    prop.transferSourceFunc(0, 16, np.zeros(0, np.int32),
+                            np.zeros((0, 16), np.float32))
+    prop.source_prop_device(1, 10)
+    prop.synchronize()
