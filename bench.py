@@ -16,7 +16,9 @@ the RTM adjoint (sourceProp + rtmAdjoint) of configuration c2 (256^3 model,
 
 ``--impl reference`` times the reference CPU implementation instead (the
 compiled reference where it exists on this machine, else the oracle port).
-Multi-GPU: shots are independent, so N ranks run N shots (weak scaling).
+Multi-GPU: shots are independent, so N ranks run N shots (weak scaling);
+each step ends with the images summed over the ranks (one NCCL all-reduce,
+the only exchange an RTM over shots needs).
 
 Other configurations print their own line:
   --config c3  one 624^3 shot (512^3 model at 8 m, jt = 2, nt = 2999) per
@@ -305,6 +307,8 @@ def run_gpu_arm(args):
         prop.rtm_adjoint_device(jt, nt, swap=1)
         if ev:
             ev[3].record(stream)
+        if world > 1:  # the shots' images summed over the ranks (NCCL)
+            born.stack_image(prop)
 
     for _ in range(args.warmup):
         device_step()
@@ -405,7 +409,9 @@ def run_gpu_arm(args):
                        "storage": args.storage or "f32",
                        "l2": "inputs larger than L2 (7 x %.0f MB fields)" %
                              (nx * ny * nz * 4 / 1e6),
-                       "parallelism": f"shots x{world} (one per GPU)"},
+                       "parallelism": f"shots x{world} (one per GPU)" +
+                       (", image summed over the ranks every step (NCCL "
+                        "all-reduce)" if world > 1 else "")},
             "roofline": roofline, "phases": phases, "tile_cfg": tiles,
             "clocks": clk.summary(), "gpu_launches": launches,
             "e2e": e2e, "cpu_baseline": cpu, "fused_fma": fused,

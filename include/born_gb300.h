@@ -177,6 +177,12 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
 /* Device results and state transfers (host arrays of n1*n2*n3 floats, or
  * npts*nt_big for traces) */
 int born_get_image(born_handle *h, float *img_out);
+/* Device address of the image (n1*n2*n3 floats on the handle's device,
+ * written on the handle's stream; valid until the next create_space or
+ * destroy), for stacking images across shots and GPUs without a host copy
+ * (the reference sums shot images on the host, util/Add).  Null without a
+ * grid. */
+float *born_image_device(born_handle *h);
 int born_get_traces(born_handle *h, float *traces_out);
 int born_get_source_levels(born_handle *h, float *p0_out, float *p1_out);
 int born_set_source_levels(born_handle *h, const float *p0, const float *p1);

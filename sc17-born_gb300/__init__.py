@@ -79,6 +79,7 @@ _SIGS = {
     "born_lin_forward": (C.c_int, [_vp, C.c_int, C.c_int, _fp]),
     "born_lin_adjoint": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _fp]),
     "born_get_image": (C.c_int, [_vp, _fp]),
+    "born_image_device": (_vp, [_vp]),
     "born_get_traces": (C.c_int, [_vp, _fp]),
     "born_get_source_levels": (C.c_int, [_vp, _fp, _fp]),
     "born_set_source_levels": (C.c_int, [_vp, _fp, _fp]),
@@ -213,6 +214,7 @@ class Handle:
         if rc != BORN_OK:
             raise BornError(rc, f"born_create(device={device}) failed")
         self.h = h
+        self.device = device
 
     def check(self, rc: int) -> int:
         if rc != BORN_OK:
@@ -413,6 +415,23 @@ class Gb300Prop(Handle):
         self.check(self.lib.born_get_image(self.h, fptr(out)))
         return out
 
+    def image_tensor(self):
+        """The device image as a torch tensor without a copy (shape
+        ``self.shape``, float32, on this handle's device).  It aliases the
+        handle's buffer: synchronize the handle before reading it on another
+        stream, and do not keep it past the next createSpace."""
+        import torch
+        ptr = self.lib.born_image_device(self.h)
+        if not ptr:
+            raise BornError(-4, "no grid (createSpace first)")
+
+        class _View:  # __cuda_array_interface__ (version 3) of the buffer
+            __cuda_array_interface__ = {
+                "shape": tuple(self.shape), "typestr": "<f4",
+                "data": (int(ptr), False), "version": 3, "strides": None,
+                "stream": None}
+        return torch.as_tensor(_View(), device=f"cuda:{self.device}")
+
     def get_traces(self, like):
         out = np.empty_like(like, dtype=np.float32)
         self.check(self.lib.born_get_traces(self.h, fptr(out)))
@@ -420,6 +439,34 @@ class Gb300Prop(Handle):
 
     def zero_traces(self):
         self.check(self.lib.born_zero_traces(self.h))
+
+
+# ---------------------------------------------------------------------------
+# Stacking images across ranks
+
+def stack_tensor(t, group=None):
+    """Sums a tensor over the ranks of ``torch.distributed`` in place (NCCL
+    for CUDA tensors, gloo for CPU ones); a no-op without a process group or
+    with one rank.  Shots are independent, so this sum is the only exchange
+    a multi-GPU RTM needs: each rank migrates its own shots and the image is
+    the sum of theirs (the reference sums shot images on the host,
+    util/Add)."""
+    import torch
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and \
+            dist.get_world_size(group) > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+        if t.is_cuda:  # the buffer may be reused on another stream next
+            torch.cuda.current_stream(t.device).synchronize()
+    return t
+
+
+def stack_image(prop, group=None):
+    """The RTM image of ``prop`` (a Gb300Prop after rtm_adjoint) summed over
+    the ranks, on the device, without a host copy; returns the tensor view of
+    the handle's image buffer, which then holds the stacked image."""
+    prop.synchronize()
+    return stack_tensor(prop.image_tensor(), group)
 
 
 # ---------------------------------------------------------------------------

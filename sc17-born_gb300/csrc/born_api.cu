@@ -1145,6 +1145,10 @@ int born_get_image(born_handle *h, float *img_out) {
   return check_device_error(h);
 }
 
+float *born_image_device(born_handle *h) {
+  return (h && h->have_space) ? h->img : nullptr;
+}
+
 int born_get_traces(born_handle *h, float *out) {
   int rc = check_ready(h);
   if (rc) return rc;

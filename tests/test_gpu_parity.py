@@ -163,3 +163,16 @@ def test_call_sequence_errors_are_status_codes(gpu):
                             np.zeros((0, 16), np.float32))
     prop.source_prop_device(1, 10)
     prop.synchronize()
+
+
+def test_device_image_view_and_single_rank_stack(gpu, po):
+    c = cases.make_case(91, shape=(20, 24, 28), nt=30, jt=1,
+                        sinc=po.sinc_table)
+    prop = gpu.Gb300Prop()
+    got = po.run_case(prop, c, which="adjoint")
+    t = prop.image_tensor()  # the handle's image buffer, no copy
+    assert t.is_cuda and tuple(t.shape) == c["shape"]
+    assert np.array_equal(t.cpu().numpy(), prop.get_image())
+    assert np.array_equal(t.cpu().numpy(), got["image"])
+    # without a process group the stack is the image itself
+    assert np.array_equal(gpu.stack_image(prop).cpu().numpy(), got["image"])

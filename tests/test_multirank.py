@@ -49,3 +49,34 @@ def test_two_gloo_ranks_shard_shots_and_take_max_time():
     assert res[0][0] == 0 and res[1][0] == 1          # one shot per rank
     assert res[0][1] == res[1][1] == 150.0             # max over ranks
     assert abs(res[0][2] - 2 * 1e9 * 2 / 0.150 / 1e9) < 1e-9  # weak scaling
+
+
+def _stack_worker(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    import importlib.util
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    pkg = os.path.join(root, "sc17-born_gb300")
+    spec = importlib.util.spec_from_file_location(
+        "born_gb300", os.path.join(pkg, "__init__.py"),
+        submodule_search_locations=[pkg])
+    born = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(born)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    # each rank's "image" of its own shot; the stack is their sum
+    img = torch.arange(24, dtype=torch.float32).reshape(2, 3, 4) * (rank + 1)
+    born.stack_tensor(img)
+    out[rank] = img.numpy().tolist()
+    dist.destroy_process_group()
+
+
+def test_image_stack_sums_the_ranks_shots():
+    world = 2
+    port = _free_port()
+    with mp.Manager() as m:
+        out = m.dict()
+        mp.spawn(_stack_worker, args=(world, port, out), nprocs=world,
+                 join=True)
+        res = dict(out)
+    want = (torch.arange(24, dtype=torch.float32).reshape(2, 3, 4) * 3)
+    for r in range(world):
+        assert torch.equal(torch.tensor(res[r]), want)
