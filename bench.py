@@ -22,8 +22,8 @@ the only exchange an RTM over shots needs).
 
 Other configurations print their own line:
   --config c3  one 624^3 shot (512^3 model at 8 m, jt = 2, nt = 2999) per
-               level storage (--storage f32,bf16,f16), 16-bit results
-               compared with the FP32 result of the same run
+               level storage (--storage f32,f32fma,bf16,f16; default
+               f32,bf16,f16), results compared with the first storage's
   --config c4  48 shots of uneven aperture advanced together (one launch per
                step, time loops as CUDA graphs) against the same shots one
                after another (--storage for the level storage)
@@ -587,7 +587,8 @@ def run_storage(args):
     nt, jt = case["nt"], case["jts"]
     n_int = wl.interior_cells(case["shape"])
     # compulsory bytes per interior cell of the three loops (fields 4 or 2 B)
-    bpc = {"f32": (32, 16, 40), "bf16": (20, 10, 28), "f16": (20, 10, 28)}
+    bpc = {"f32": (32, 16, 40), "f32fma": (32, 16, 40), "bf16": (20, 10, 28),
+           "f16": (20, 10, 28)}
     res, ref = {}, None
     for st in args.storage.split(","):
         prop = born.Gb300Prop(0)
