@@ -47,6 +47,48 @@ def build_ref(force: bool = False) -> str | None:
     return REF_SO
 
 
+REF_GEOM_SO = os.path.join(HERE, "_ref", "libref_geom.so")
+_ref_geom = None
+
+
+def ref_geom_lib():
+    """The reference's own geometry and glue code (vel_fd_3d::rand_subspace,
+    set_compute_size, the wavelet reader and source points, map_data,
+    laplac, deriv), compiled from its sources with oracle/ref_geom_shim.cc,
+    or None where the sources are absent."""
+    global _ref_geom
+    if _ref_geom is None:
+        if os.path.isdir(os.path.join(REF_SRC, "base")) and \
+                not os.path.exists(REF_GEOM_SO):
+            subprocess.run(["make", "-s", "-C", HERE, "_ref/libref_geom.so",
+                            f"REF={REF_SRC}"], check=True)
+        if not os.path.exists(REF_GEOM_SO):
+            return None
+        lib = C.CDLL(REF_GEOM_SO)
+        i, f = C.c_int, C.c_float
+        sig = {
+            "ref_geom_compute_size": (i, [i, i, i]),
+            "ref_geom_rand_subspace": (i, [_fp, i, i, i] + [f] * 6 +
+                                       [i, i, i, i, f, i, i, i] + [f] * 6 +
+                                       [_fp]),
+            "ref_geom_source": (i, [_fp, i, f, f, f, f] + [f] * 6 +
+                                [i, i, i, i, _ip, _fp]),
+            "ref_geom_map_locs": (i, [i, _fp, _fp, _fp, i, i, _ip]),
+            "ref_geom_receivers": (i, [i, i] + [f] * 11 + [i, i, i, i, _ip]),
+            "ref_geom_calc_stability": (i, [_fp, i, i, i, f, f, f, f, i, _fp,
+                                            _ip]),
+            "ref_geom_map_data": (i, [i, i, _fp, _fp, i, i, i, i]),
+            "ref_geom_laplac": (i, [i, i, _fp, _fp, i, i, i]),
+            "ref_geom_deriv": (i, [i, i, _fp, _fp, i, i, i, f]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _ref_geom = lib
+    return _ref_geom
+
+
 def _f32(a):
     return np.ascontiguousarray(a, dtype=np.float32)
 

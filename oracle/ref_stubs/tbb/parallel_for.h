@@ -13,8 +13,15 @@ inline int oracle_ref_threads() {
   }();
   return n;
 }
+// Built with ORACLE_REF_SERIAL the range runs in order on one thread (the
+// reference's random boundary draws rand() inside a parallel_for, so only
+// a serial run is reproducible).
 template <class T, class F>
 void parallel_for(const blocked_range<T> &r, const F &f) {
+#ifdef ORACLE_REF_SERIAL
+  f(r);
+  return;
+#endif
   const int nt = oracle_ref_threads();
   const long long len = (long long)(r.end() - r.begin());
   if (nt <= 1 || len < 2 * nt) {

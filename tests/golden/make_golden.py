@@ -47,6 +47,23 @@ def main():
             **{f"par_{k}": v for k, v in scalars.items()},
             **{f"out_{k}": v for k, v in out.items()})
         print(name, {k: float(np.linalg.norm(v)) for k, v in out.items()})
+    make_geometry()
+
+
+def make_geometry():
+    """Outputs of the reference's geometry and glue code (compiled from its
+    own sources into oracle/_ref/libref_geom.so) on the seeded inputs of
+    tests/geometry_cases.py; the inputs are regenerated from the seed."""
+    import geometry_cases as gc
+    if po.ref_geom_lib() is None:
+        sys.exit("reference sources not available: cannot make fixtures")
+    out = gc.run(gc.make_inputs(GEOMETRY_SEED), po, ref=True)
+    np.savez_compressed(os.path.join(HERE, "geometry.npz"),
+                        seed=np.array(GEOMETRY_SEED), **out)
+    print("geometry", sorted(out))
+
+
+GEOMETRY_SEED = 0
 
 
 if __name__ == "__main__":

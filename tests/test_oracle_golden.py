@@ -93,3 +93,30 @@ def test_primitives_against_compiled_reference(po):
         outs.append((a, b))
     assert np.array_equal(outs[0][0], outs[1][0])
     assert np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_geometry_matches_reference_fixture(po):
+    """Source points and wavelet derivative, receiver cells, compute-grid
+    sizes, the random boundary, the FD step and the linear glue (laplac,
+    deriv, map_data) of the oracle against the outputs of the reference's
+    own code on the same seeded inputs (tests/golden/geometry.npz)."""
+    import geometry_cases as gc
+    z = np.load(os.path.join(GOLDEN, "geometry.npz"))
+    got = gc.run(gc.make_inputs(int(z["seed"])), po, ref=False)
+    names = [k for k in z.files if k != "seed"]
+    assert sorted(names) == sorted(got)
+    for k in names:
+        assert got[k].shape == z[k].shape, k
+        assert np.array_equal(got[k], z[k]), f"{k} differs from the reference"
+
+
+def test_geometry_against_compiled_reference_random_cases(po):
+    if po.ref_geom_lib() is None:
+        pytest.skip("reference sources not present")
+    import geometry_cases as gc
+    for seed in (1, 2):
+        inp = gc.make_inputs(seed)
+        a = gc.run(inp, po, ref=True)
+        b = gc.run(inp, po, ref=False)
+        for k in a:
+            assert np.array_equal(a[k], b[k]), (seed, k)
