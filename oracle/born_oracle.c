@@ -379,3 +379,10 @@ void oracle_add_image(float *whole, int w1, int w2, int w3, const float *sub,
     }
   }
 }
+
+/* image_rtm_3d.cc:33-35 (and :64-66): f = (int)((sub.o - whole.o) / whole.d)
+ * with the axes' float origins and spacing. */
+int oracle_window_offset(float o_sub, float o_whole, float d_whole) {
+  const float diff = o_sub - o_whole;
+  return (int)(diff / d_whole);
+}

@@ -159,6 +159,9 @@ void oracle_extract_sub(const float *whole, int w1, int w2, int w3, float *sub,
                         int s1, int s2, int s3, int f1, int f2, int f3);
 void oracle_add_image(float *whole, int w1, int w2, int w3, const float *sub,
                       int s1, int s2, int s3, int f1, int f2, int f3);
+/* window offset of one axis from the axes' origins and the whole image's
+ * spacing (base/image_rtm_3d.cc:33-35, :64-66): float, truncated */
+int oracle_window_offset(float o_sub, float o_whole, float d_whole);
 
 #ifdef __cplusplus
 }

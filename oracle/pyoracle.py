@@ -32,8 +32,10 @@ _ip = C.POINTER(C.c_int)
 
 
 def build_port(force: bool = False) -> str:
-    if force or not os.path.exists(PORT_SO):
-        subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    # make rebuilds only what is older than its sources
+    subprocess.run(["make", "-s", "-C", HERE, "port"] + (["-B"] if force
+                                                          else []),
+                   check=True)
     return PORT_SO
 
 
@@ -58,8 +60,7 @@ def ref_geom_lib():
     or None where the sources are absent."""
     global _ref_geom
     if _ref_geom is None:
-        if os.path.isdir(os.path.join(REF_SRC, "base")) and \
-                not os.path.exists(REF_GEOM_SO):
+        if os.path.isdir(os.path.join(REF_SRC, "base")):
             subprocess.run(["make", "-s", "-C", HERE, "_ref/libref_geom.so",
                             f"REF={REF_SRC}"], check=True)
         if not os.path.exists(REF_GEOM_SO):
@@ -80,6 +81,8 @@ def ref_geom_lib():
             "ref_geom_map_data": (i, [i, i, _fp, _fp, i, i, i, i]),
             "ref_geom_laplac": (i, [i, i, _fp, _fp, i, i, i]),
             "ref_geom_deriv": (i, [i, i, _fp, _fp, i, i, i, f]),
+            "ref_geom_image_window": (i, [i, _fp, i, i, i] + [f] * 6 +
+                                      [_fp, i, i, i] + [f] * 6),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -202,6 +205,7 @@ def port_lib():
             "oracle_add_image": (None, [_fp, C.c_int, C.c_int, C.c_int, _fp,
                                         C.c_int, C.c_int, C.c_int, C.c_int,
                                         C.c_int, C.c_int]),
+            "oracle_window_offset": (C.c_int, [C.c_float] * 3),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)

@@ -4,7 +4,8 @@
  * oracle/_ref/libref_geom.so): vel_fd_3d::rand_subspace, source_func::
  * set_compute_size / wavelet_source_func (wavelet derivative and source
  * points), map_data (receiver cells, trace lead), fd_prop::calc_stability
- * (FD time step and step count), laplac and deriv.  Test
+ * (FD time step and step count), image_rtm_3d's window (extract_sub,
+ * add_image), laplac and deriv.  Test
  * infrastructure only: used to pin the oracle's restatement of these pieces
  * and to generate golden fixtures.  The reference reads its arrays through
  * SEP files; here they are in-memory arrays registered with the stand-in
@@ -24,6 +25,7 @@
 #include "deriv_3d.h"
 #include "fd_prop_3d.h"
 #include "float_3d.h"
+#include "image_rtm_3d.h"
 #include "laplac_3d.h"
 #include "map_data_3d.h"
 #include "source_func_3d.h"
@@ -38,6 +40,14 @@ void oc_float::tagInit(std::string tag) {
 }
 void oc_float::readAll(std::shared_ptr<hypercube_float> h) {
   _file->readFloatStream(h->vals, h->getN123());
+}
+// a "new" file is the in-memory file registered under the tag beforehand
+void oc_float::initNewFile(std::string tag, std::shared_ptr<SEP::genericIO> io,
+                           std::shared_ptr<SEP::hypercube>,
+                           const SEP::usage_code usage) {
+  _io = io;
+  _tag = tag;
+  _file = _io->getRegFile(tag, usage);
 }
 #define ORACLE_NOT_USED std::abort()
 std::shared_ptr<my_vector> oc_float::clone_vec() { ORACLE_NOT_USED; }
@@ -271,6 +281,37 @@ int ref_geom_deriv(int adjoint, int add, float *m, float *d, int n1, int n2,
   for (long long i = 0; i < n; ++i) {
     m[i] = mv->vals[i];
     d[i] = dv->vals[i];
+  }
+  return 0;
+}
+
+// image_rtm_3d::extract_sub (extract != 0: whole -> sub) or add_image
+// (whole += sub) for a window given by its axes; the whole image's axes are
+// those of the velocity file, as in the image_rtm_3d constructor
+int ref_geom_image_window(int extract, float *whole, int w1, int w2, int w3,
+                          float wo1, float wo2, float wo3, float wd1,
+                          float wd2, float wd3, float *sub, int s1, int s2,
+                          int s3, float so1, float so2, float so3, float sd1,
+                          float sd2, float sd3) {
+  QuietStderr q;
+  const auto wax = axes3(w1, w2, w3, wo1, wo2, wo3, wd1, wd2, wd3);
+  SEP::genericIO::register_file("oracle_image_vel", wax, whole);
+  SEP::genericIO::register_file("oracle_image", wax, whole);
+  auto io = std::make_shared<SEP::genericIO>();
+  auto v = std::make_shared<vel_fd_3d>(io, "oracle_image_vel");
+  image_rtm_3d img(io, "oracle_image", v);
+  const long long nw = (long long)w1 * w2 * w3, ns = (long long)s1 * s2 * s3;
+  if (extract) {
+    auto out = img.extract_sub(SEP::axis(s1, so1, sd1), SEP::axis(s2, so2, sd2),
+                               SEP::axis(s3, so3, sd3));
+    for (long long i = 0; i < ns; ++i) sub[i] = out->vals[i];
+  } else {
+    for (long long i = 0; i < nw; ++i) img.image->vals[i] = whole[i];
+    auto part = std::make_shared<hypercube_float>(
+        axes3(s1, s2, s3, so1, so2, so3, sd1, sd2, sd3));
+    for (long long i = 0; i < ns; ++i) part->vals[i] = sub[i];
+    img.add_image(part);
+    for (long long i = 0; i < nw; ++i) whole[i] = img.image->vals[i];
   }
   return 0;
 }

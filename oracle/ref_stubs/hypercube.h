@@ -4,6 +4,7 @@
  * fastest axis. */
 #pragma once
 #include <memory>
+#include <sstream>
 #include <vector>
 
 #include "axis.h"
@@ -24,6 +25,8 @@ class hypercube {
     return a;
   }
   int getNdim() const { return (int)axes_.size(); }
+  // description text; the reference prints it only on paths not taken here
+  void infoStream(std::stringstream &) const {}
   long long getN123() const {
     long long n = 1;
     for (const axis &a : axes_) n *= a.n;

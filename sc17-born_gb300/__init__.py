@@ -149,6 +149,7 @@ _SIGS = {
                                    C.c_int]),
     "born_add_image": (C.c_int, [_fp, C.c_int, C.c_int, C.c_int, _fp, C.c_int,
                                  C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
+    "born_window_offset": (C.c_int, [C.c_float] * 3),
     "born_sep_read_info": (C.c_int, [C.c_char_p, _vp]),
     "born_sep_read": (C.c_int, [C.c_char_p, _fp, C.c_longlong]),
     "born_sep_write": (C.c_int, [C.c_char_p, _vp, _fp, C.c_int]),

@@ -309,4 +309,9 @@ int born_add_image(float *whole, int w1, int w2, int w3, const float *sub,
   return BORN_OK;
 }
 
+int born_window_offset(float o_sub, float o_whole, float d_whole) {
+  const float diff = o_sub - o_whole;
+  return (int)(diff / d_whole);
+}
+
 }  // extern "C"

@@ -82,6 +82,12 @@ int born_extract_sub(const float *whole, int w1, int w2, int w3, float *sub,
                      int s1, int s2, int s3, int f1, int f2, int f3);
 int born_add_image(float *whole, int w1, int w2, int w3, const float *sub,
                    int s1, int s2, int s3, int f1, int f2, int f3);
+/* Sample offset of a window axis within the whole image's axis, as
+ * image_rtm_3d.cc:33-35 and :64-66 form it from the two axes: (o_sub -
+ * o_whole) / d_whole in float, truncated toward zero.  For origins that are
+ * not exact multiples of the spacing this can be one sample short of the
+ * rounded value; the window functions above take the offsets it returns. */
+int born_window_offset(float o_sub, float o_whole, float d_whole);
 
 /* SEP regular files (the reference's genericIO datasets): header text of
  * key=value pairs (n1..n6, o1..o6, d1..d6, esize=4, data_format xdr_float or

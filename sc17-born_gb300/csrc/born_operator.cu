@@ -220,7 +220,11 @@ struct born_op {
   // compute grid
   int n1 = 0, n2 = 0, n3 = 0;
   float o1 = 0, o2 = 0, o3 = 0;
-  int f = 0;  // model origin inside the compute grid, in samples
+  int f = 0;  // boundary cells on each side of the model (nbound + fat)
+  // model-grid sample of the compute grid's first cell per axis, as the
+  // image window forms it from the two axes (image_rtm_3d.cc:33-35): -f, or
+  // -f + 1 where the float origins truncate (spacings such as 10.1)
+  int w1 = 0, w2 = 0, w3 = 0;
   float dt = 0;
   int jt = 1, nt = 0, nt_big = 0;
   std::vector<float> table;  // jt x 8
@@ -317,6 +321,9 @@ int born_op_create(born_handle *h, const born_op_params *p,
   op->o1 = p->o1 - p->d1 * op->f;
   op->o2 = p->o2 - p->d2 * op->f;
   op->o3 = p->o3 - p->d3 * op->f;
+  op->w1 = born_window_offset(op->o1, p->o1, p->d1);
+  op->w2 = born_window_offset(op->o2, p->o2, p->d2);
+  op->w3 = born_window_offset(op->o3, p->o3, p->d3);
   op->nt_big = p->nt_data + 8;
   op->table.resize((size_t)op->jt * 8);
   born_sinc_table(op->jt, 8, op->table.data());
@@ -435,8 +442,8 @@ int born_op_forward(born_op *op, int add, const float *model, float *data) {
     if (rc) return rc;
     // img = laplac(window(model)) on the compute grid (rtm_zero_op_3d.cc:161-180)
     k_extract_window<<<grid_for(n123), kThreads, 0, h->stream>>>(
-        model, p.n1, p.n2, p.n3, h->img, h->n1, h->n2, h->n3, -op->f, -op->f,
-        -op->f);
+        model, p.n1, p.n2, p.n3, h->img, h->n1, h->n2, h->n3, op->w1, op->w2,
+        op->w3);
     k_laplac_fwd<<<grid_for(n123), kThreads, 0, h->stream>>>(h->img, h->refl,
                                                              n12, n123, 0);
     OPCK(op, cudaGetLastError());
@@ -495,8 +502,8 @@ int born_op_adjoint(born_op *op, int add, float *model, const float *data) {
     k_laplac_adj<<<grid_for(n123), kThreads, 0, h->stream>>>(h->refl, h->img,
                                                              n12, n123, 0);
     k_add_window<<<grid_for(n123), kThreads, 0, h->stream>>>(
-        model, p.n1, p.n2, p.n3, h->refl, h->n1, h->n2, h->n3, -op->f, -op->f,
-        -op->f);
+        model, p.n1, p.n2, p.n3, h->refl, h->n1, h->n2, h->n3, op->w1, op->w2,
+        op->w3);
     OPCK(op, cudaGetLastError());
     h->launches += 2;
     h->have_refl = false;

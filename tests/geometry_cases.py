@@ -3,7 +3,7 @@ and one runner that applies either the reference's own compiled code
 (oracle/_ref/libref_geom.so: fd_prop::calc_stability,
 source_func::set_compute_size, the wavelet reader and source points,
 vel_fd_3d::rand_subspace, data_rtm_3d::get_source_func + map_data receiver
-cells, map_data, laplac, deriv) or the oracle's restatement to them, so that
+cells, image_rtm_3d's window, map_data, laplac, deriv) or the oracle's restatement to them, so that
 the two can be compared bit for bit (tests/test_oracle_golden.py) and the
 reference's outputs stored as fixtures (tests/golden/make_golden.py)."""
 import ctypes as C
@@ -21,6 +21,26 @@ REC_GRID = dict(n=(64, 56, 40), o=(-60.0, -60.0, -60.0), d=(10.0, 10.0, 10.0),
 OP_SHAPE = (9, 7, 11)             # n3, n2, n1 for laplac / deriv
 MAP_SHAPE = dict(nt=20, ntb=28, n2=5, n3=3)
 DERIV_D1 = 0.002
+WIN_WHOLE = (12, 10, 9)          # n1, n2, n3 of the whole image
+
+
+def window_cases():
+    """(whole origins, whole spacings, window sizes, window origins): a
+    window around the image, inside it, over its far edge, and three on
+    origins that are not multiples of the spacing (float truncation toward
+    zero, on both sides)."""
+    f32 = np.float32
+    wo, wd = (0.0, 0.0, 0.0), (10.0, 10.0, 10.0)
+    oo = tuple(f32(x) for x in (13.7, -2.3, 0.1))
+    od = tuple(f32(x) for x in (7.3, 6.1, 9.7))
+    return [
+        (wo, wd, (16, 14, 13), (-20.0, -20.0, -20.0)),
+        (wo, wd, (5, 4, 3), (30.0, 20.0, 10.0)),
+        (wo, wd, (6, 5, 4), (90.0, 70.0, 60.0)),
+        (oo, od, (14, 12, 11), tuple(o - f32(2) * d for o, d in zip(oo, od))),
+        (oo, od, (5, 4, 3), tuple(o + f32(3.5) * d for o, d in zip(oo, od))),
+        (oo, od, (6, 5, 5), tuple(o - f32(3.5) * d for o, d in zip(oo, od))),
+    ]
 
 
 def make_inputs(seed: int = 0) -> dict:
@@ -41,6 +61,9 @@ def make_inputs(seed: int = 0) -> dict:
         "map_d": rng.standard_normal(
             (MAP_SHAPE["n3"], MAP_SHAPE["n2"], MAP_SHAPE["nt"])).astype(
                 np.float32),
+        "win_whole": rng.standard_normal(WIN_WHOLE[::-1]).astype(np.float32),
+        "win_sub": [rng.standard_normal(c[2][::-1]).astype(np.float32)
+                    for c in window_cases()],
         "rec_cfg": np.array([(16, 12, 40.0, 20.0, 30.0, 20.0, 10.0),
                              (7, 9, 13.7, 7.3, 21.1, 11.9, 14.2)], np.float32),
         "stab_cfg": np.array([(4500.0, 10.0, 0.001, 2000),
@@ -129,6 +152,29 @@ def run(inp: dict, po, ref: bool) -> dict:
                                          int(ntd), C.byref(nt))
             stab.append((float(np.float32(dt)), nt.value))
     out["stability"] = np.array(stab, np.float64)
+
+    # image window: extract_sub and add_image with offsets from the axes
+    w1, w2, w3 = WIN_WHOLE
+    for k, (wo, wd, sn, so) in enumerate(window_cases()):
+        wo, wd, so = ([float(x) for x in t] for t in (wo, wd, so))
+        for extract in (1, 0):
+            whole = inp["win_whole"].copy()
+            sub = (np.zeros(sn[::-1], np.float32) if extract
+                   else inp["win_sub"][k].copy())
+            if ref:
+                R.ref_geom_image_window(extract, f(whole), w1, w2, w3, *wo,
+                                        *wd, f(sub), *sn, *so, *wd)
+            else:
+                off = [L.oracle_window_offset(so[a], wo[a], wd[a])
+                       for a in range(3)]
+                if extract:
+                    L.oracle_extract_sub(f(whole), w1, w2, w3, f(sub), *sn,
+                                         *off)
+                else:
+                    L.oracle_add_image(f(whole), w1, w2, w3, f(sub), *sn,
+                                       *off)
+            out[f"win_{'ext' if extract else 'add'}_{k}"] = \
+                sub if extract else whole
 
     # the linear glue: laplac, deriv, map_data (forward and adjoint, with and
     # without accumulation)

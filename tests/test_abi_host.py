@@ -166,3 +166,15 @@ def test_linear_glue_matches_oracle(born, po):
     P.oracle_add_image(po.fptr(wb), 8, 7, 6, po.fptr(sub_b), 9, 9, 9, -2, -1,
                        -3)
     assert np.array_equal(wa, wb)
+    # window offsets from float origins (truncation toward zero on both
+    # sides, and the compute grids of 4-55 boundary cells at odd spacings)
+    f32 = np.float32
+    trip = [(float(f32(o) - f32(d) * f32(k)), o, d)
+            for o in (0.0, 13.7, -2.3) for d in (10.0, 10.1, 10.3, 8.33, 7.3)
+            for k in range(4, 56)]
+    trip += [tuple(float(f32(x)) for x in rng.uniform(-500, 500, 2)) +
+             (float(f32(rng.uniform(1, 20))),) for _ in range(500)]
+    got = [L.born_window_offset(*t) for t in trip]
+    assert got == [P.oracle_window_offset(*t) for t in trip]
+    assert L.born_window_offset(float(f32(-10.3) * f32(14)), 0.0, 10.3) == -13
+    assert L.born_window_offset(-35.0, 0.0, 10.0) == -3  # not floor (-4)

@@ -30,10 +30,10 @@ def torch_cuda(born):
     return torch
 
 
-def setup_problem(seed=7, n=(20, 22, 24), nbound=6, nt_data=60, nshots=2):
+def setup_problem(seed=7, n=(20, 22, 24), nbound=6, nt_data=60, nshots=2,
+                  d=10.0):
     rng = np.random.default_rng(seed)
     n3, n2, n1 = n
-    d = 10.0
     z = np.arange(n3)[:, None, None]
     vel = (2000.0 + 40.0 * z + 100 * rng.random(n)).astype(np.float32)
     shots = np.array([[d * (n1 // 2 + k), d * (n2 // 2), 20.0]
@@ -63,7 +63,10 @@ def oracle_operator(po, kw, model=None, data=None):
     jt = int(np.float32(kw["dt_data"]) / np.float32(dt))  # float / float
     nc = [L.oracle_compute_size(m, nb, 4) for m in (n1, n2, n3)]
     f = nb + 4
-    oc = -d * f
+    # compute-grid origin o + (-d * f) in float (source_func_3d.cc:65-67) and
+    # the image window's offset formed from it (image_rtm_3d.cc:33-35)
+    oc = float(np.float32(0) + np.float32(-d) * np.float32(f))
+    w = L.oracle_window_offset(oc, 0.0, d)
     tab = po.sinc_table(jt)
     wav = np.ascontiguousarray(kw["wavelet"])
     wd = np.zeros_like(wav)
@@ -103,7 +106,7 @@ def oracle_operator(po, kw, model=None, data=None):
         if model is not None:
             img = np.zeros(shape_c, np.float32)
             L.oracle_extract_sub(po.fptr(model), n1, n2, n3, po.fptr(img),
-                                 nc[0], nc[1], nc[2], -f, -f, -f)
+                                 nc[0], nc[1], nc[2], w, w, w)
             lap = np.zeros(shape_c, np.float32)
             L.oracle_laplac_forward(0, po.fptr(img), po.fptr(lap), nc[0],
                                     nc[1], nc[2])
@@ -137,7 +140,7 @@ def oracle_operator(po, kw, model=None, data=None):
             L.oracle_laplac_adjoint(0, po.fptr(lap), po.fptr(img), nc[0],
                                     nc[1], nc[2])
             L.oracle_add_image(po.fptr(out), n1, n2, n3, po.fptr(lap), nc[0],
-                               nc[1], nc[2], -f, -f, -f)
+                               nc[1], nc[2], w, w, w)
     return out
 
 
@@ -163,6 +166,29 @@ def test_reference_operator_matches_oracle_chain(born, po, torch_cuda):
     assert rel(ma.cpu().numpy(), 2 * got) <= 1e-6
     op.adjoint(False, ma, torch.from_numpy(data).cuda())
     assert rel(ma.cpu().numpy(), got) == 0.0
+
+
+def test_reference_operator_window_from_float_origins(born, po, torch_cuda):
+    """At 10.3 m spacing and 10 boundary cells the compute grid starts at
+    -144.2 m, which the reference's image window truncates to sample -13,
+    not -14; the operator windows the model there too."""
+    torch = torch_cuda
+    kw = setup_problem(seed=5, nbound=10, nt_data=40, nshots=1, d=10.3)
+    L = po.port_lib()
+    oc = float(np.float32(-10.3) * np.float32(14))
+    assert L.oracle_window_offset(oc, 0.0, 10.3) == -13
+    op = born.BornOperator(**kw)
+    rng = np.random.default_rng(12)
+    m = rng.standard_normal(op.model_shape).astype(np.float32)
+    dd = torch.zeros(op.data_shape, device="cuda")
+    op.forward(False, torch.from_numpy(m).cuda(), dd)
+    want = oracle_operator(po, kw, model=m)
+    assert rel(dd.cpu().numpy(), want) <= 1e-5
+    data = rng.standard_normal(op.data_shape).astype(np.float32)
+    ma = torch.zeros(op.model_shape, device="cuda")
+    op.adjoint(False, ma, torch.from_numpy(data).cuda())
+    want = oracle_operator(po, kw, data=data)
+    assert rel(ma.cpu().numpy(), want) <= 1e-6
 
 
 def test_exact_operator_dot_product(born, torch_cuda):
