@@ -289,100 +289,180 @@ __device__ __forceinline__ void st4(float *p, const float4 &v) {
   *reinterpret_cast<float4 *>(p) = v;
 }
 
+// Packed FP32 pairs (add/sub/mul/fma.rn.f32x2, sm_100 family): one
+// instruction rounds each lane exactly as the scalar form does (IEEE
+// round-to-nearest, subnormals kept; checked lane by lane on sm_103a).  A
+// pair is two adjacent 32-bit registers: the (x, y) and (z, w) halves of a
+// float4 are pairs as loaded.  One caveat decides where they may be used in
+// the reference-order arithmetic: the compiler contracts a packed multiply
+// whose result feeds a packed add or subtract into a packed fused
+// multiply-add, whatever the rounding modifier or -fmad setting (measured on
+// sm_103a, also for fma(a, b, -0)), while a scalar mul.rn feeding a packed
+// add is left alone.  So the reference-order sums multiply with scalar
+// __fmul_rn (mulc2s, mul2s) and add in pairs; the fused-arithmetic paths
+// use packed multiplies and multiply-adds throughout.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float lo, float hi) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float2 upk2(f32x2 v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+// c * v and a * b lane by lane with scalar, never-contracted multiplies
+__device__ __forceinline__ f32x2 mulc2s(float c, f32x2 v) {
+  const float2 t = upk2(v);
+  return pk2(__fmul_rn(c, t.x), __fmul_rn(c, t.y));
+}
+__device__ __forceinline__ f32x2 mul2s(f32x2 a, f32x2 b) {
+  const float2 x = upk2(a), y = upk2(b);
+  return pk2(__fmul_rn(x.x, y.x), __fmul_rn(x.y, y.y));
+}
+// cells (x, x+1) (h = 0) or (x+2, x+3) (h = 1) of a float4
+__device__ __forceinline__ f32x2 cells2(const float4 &v, int h) {
+  return h == 0 ? pk2(v.x, v.y) : pk2(v.z, v.w);
+}
+__device__ __forceinline__ void set_cells2(float4 &v, int h, f32x2 x) {
+  const float2 t = upk2(x);
+  if (h == 0) {
+    v.x = t.x;
+    v.y = t.y;
+  } else {
+    v.z = t.x;
+    v.w = t.y;
+  }
+}
+// leapfrog() on a pair of cells
+__device__ __forceinline__ f32x2 leapfrog2(f32x2 vel, f32x2 s, f32x2 p,
+                                           f32x2 old) {
+  return sub2(add2(add2(mul2s(vel, s), p), p), old);
+}
+
 // Stencil sums of this thread's 4 consecutive cells (x .. x+3) of one row,
 // from a TMA box (x/y neighbours) and the register z window.  Each cell's
 // sum is formed in the reference order of cpuProp::prop (cpu_prop.cc:235-247):
 // C0 p, then the x pairs, the y pairs and the z pairs, every product and sum
-// separately rounded; the four cells advance together so that every shared
-// load is a float4 (3 for the x window, 2 per y offset).
+// separately rounded.  The four cells advance together so that every shared
+// load is a float4 (3 for the x window, 2 per y offset), as two packed pairs
+// (cells x, x+1 and x+2, x+3) whose neighbour sums and running sums are
+// packed adds; the products are scalar (see f32x2).  The x offsets of odd
+// distance need pairs that straddle the loaded float4s, built once
+// (w1..w10).
 template <int BX>
 __device__ __forceinline__ float4 stencil4(const float *box, int brow,
                                            int bcol, const float4 (&q)[9],
                                            const float *c, float4 &center) {
   const float *r = box + brow * BX + bcol;
-  float w[12];
-  {
-    const float4 L = *reinterpret_cast<const float4 *>(r - 4);
-    const float4 M = *reinterpret_cast<const float4 *>(r);
-    const float4 R = *reinterpret_cast<const float4 *>(r + 4);
-    w[0] = L.x; w[1] = L.y; w[2] = L.z; w[3] = L.w;
-    w[4] = M.x; w[5] = M.y; w[6] = M.z; w[7] = M.w;
-    w[8] = R.x; w[9] = R.y; w[10] = R.z; w[11] = R.w;
-    center = M;
-  }
-  float s[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    s[j] = __fmul_rn(c[0], w[4 + j]);
-    s[j] = __fadd_rn(s[j], __fmul_rn(c[2], __fadd_rn(w[3 + j], w[5 + j])));
-    s[j] = __fadd_rn(s[j], __fmul_rn(c[5], __fadd_rn(w[2 + j], w[6 + j])));
-    s[j] = __fadd_rn(s[j], __fmul_rn(c[8], __fadd_rn(w[1 + j], w[7 + j])));
-    s[j] = __fadd_rn(s[j], __fmul_rn(c[11], __fadd_rn(w[0 + j], w[8 + j])));
-  }
+  const float4 L = *reinterpret_cast<const float4 *>(r - 4);
+  const float4 M = *reinterpret_cast<const float4 *>(r);
+  const float4 R = *reinterpret_cast<const float4 *>(r + 4);
+  center = M;
+  // x window w0..w11 = L, M, R: pairs starting at even w (as loaded) and at
+  // odd w
+  const f32x2 e0 = pk2(L.x, L.y), e2 = pk2(L.z, L.w), e4 = pk2(M.x, M.y),
+              e6 = pk2(M.z, M.w), e8 = pk2(R.x, R.y), e10 = pk2(R.z, R.w);
+  const f32x2 o1 = pk2(L.y, L.z), o3 = pk2(L.w, M.x), o5 = pk2(M.y, M.z),
+              o7 = pk2(M.w, R.x), o9 = pk2(R.y, R.z);
+  // cells (x, x+1): centre e4; cells (x+2, x+3): centre e6
+  f32x2 s0 = mulc2s(c[0], e4), s1 = mulc2s(c[0], e6);
+  s0 = add2(s0, mulc2s(c[2], add2(o3, o5)));
+  s1 = add2(s1, mulc2s(c[2], add2(o5, o7)));
+  s0 = add2(s0, mulc2s(c[5], add2(e2, e6)));
+  s1 = add2(s1, mulc2s(c[5], add2(e4, e8)));
+  s0 = add2(s0, mulc2s(c[8], add2(o1, o7)));
+  s1 = add2(s1, mulc2s(c[8], add2(o3, o9)));
+  s0 = add2(s0, mulc2s(c[11], add2(e0, e8)));
+  s1 = add2(s1, mulc2s(c[11], add2(e2, e10)));
   const int cy[4] = {3, 6, 9, 12}, cz[4] = {1, 4, 7, 10};
 #pragma unroll
   for (int m = 1; m <= 4; ++m) {
     const float4 u = *reinterpret_cast<const float4 *>(r - m * BX);
     const float4 d = *reinterpret_cast<const float4 *>(r + m * BX);
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      s[j] = __fadd_rn(s[j], __fmul_rn(c[cy[m - 1]],
-                                       __fadd_rn(comp(u, j), comp(d, j))));
+    const float k = c[cy[m - 1]];
+    s0 = add2(s0, mulc2s(k, add2(pk2(u.x, u.y), pk2(d.x, d.y))));
+    s1 = add2(s1, mulc2s(k, add2(pk2(u.z, u.w), pk2(d.z, d.w))));
   }
 #pragma unroll
-  for (int m = 1; m <= 4; ++m)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      s[j] = __fadd_rn(
-          s[j], __fmul_rn(c[cz[m - 1]],
-                          __fadd_rn(comp(q[4 - m], j), comp(q[4 + m], j))));
-  return make_float4(s[0], s[1], s[2], s[3]);
+  for (int m = 1; m <= 4; ++m) {
+    const float4 &u = q[4 - m], &d = q[4 + m];
+    const float k = c[cz[m - 1]];
+    s0 = add2(s0, mulc2s(k, add2(pk2(u.x, u.y), pk2(d.x, d.y))));
+    s1 = add2(s1, mulc2s(k, add2(pk2(u.z, u.w), pk2(d.z, d.w))));
+  }
+  const float2 a = upk2(s0), b = upk2(s1);
+  return make_float4(a.x, a.y, b.x, b.y);
 }
 
 // The same sums with fused multiply-adds, over the stored values of any
 // storage (16-bit values in raw units: the caller applies the level's
 // scale).  Used by every storage but the reference-order FP32 one: these
-// paths are judged by their error, not by bit equality.
+// paths are judged by their error, not by bit equality.  Packed pairs as in
+// stencil4 (fma.rn.f32x2 rounds each lane once, as fmaf does).
 template <int BX, int ST>
 __device__ __forceinline__ float4 stencil4_lp(const unsigned char *box,
                                               int brow, int bcol,
                                               const float4 (&q)[9],
                                               const float *c, float4 &center) {
   const int e = brow * BX + bcol;
-  float w[12];
-  {
-    const float4 L = ld4<ST>(box, e - 4);
-    const float4 M = ld4<ST>(box, e);
-    const float4 R = ld4<ST>(box, e + 4);
-    w[0] = L.x; w[1] = L.y; w[2] = L.z; w[3] = L.w;
-    w[4] = M.x; w[5] = M.y; w[6] = M.z; w[7] = M.w;
-    w[8] = R.x; w[9] = R.y; w[10] = R.z; w[11] = R.w;
-    center = M;
-  }
-  float s[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    s[j] = c[0] * w[4 + j];
-    s[j] = fmaf(c[2], w[3 + j] + w[5 + j], s[j]);
-    s[j] = fmaf(c[5], w[2 + j] + w[6 + j], s[j]);
-    s[j] = fmaf(c[8], w[1 + j] + w[7 + j], s[j]);
-    s[j] = fmaf(c[11], w[0 + j] + w[8 + j], s[j]);
-  }
+  const float4 L = ld4<ST>(box, e - 4);
+  const float4 M = ld4<ST>(box, e);
+  const float4 R = ld4<ST>(box, e + 4);
+  center = M;
+  const f32x2 e0 = pk2(L.x, L.y), e2 = pk2(L.z, L.w), e4 = pk2(M.x, M.y),
+              e6 = pk2(M.z, M.w), e8 = pk2(R.x, R.y), e10 = pk2(R.z, R.w);
+  const f32x2 o1 = pk2(L.y, L.z), o3 = pk2(L.w, M.x), o5 = pk2(M.y, M.z),
+              o7 = pk2(M.w, R.x), o9 = pk2(R.y, R.z);
+  auto cc = [&](int k) { return pk2(c[k], c[k]); };
+  f32x2 s0 = mul2(cc(0), e4), s1 = mul2(cc(0), e6);
+  s0 = fma2(cc(2), add2(o3, o5), s0);
+  s1 = fma2(cc(2), add2(o5, o7), s1);
+  s0 = fma2(cc(5), add2(e2, e6), s0);
+  s1 = fma2(cc(5), add2(e4, e8), s1);
+  s0 = fma2(cc(8), add2(o1, o7), s0);
+  s1 = fma2(cc(8), add2(o3, o9), s1);
+  s0 = fma2(cc(11), add2(e0, e8), s0);
+  s1 = fma2(cc(11), add2(e2, e10), s1);
   const int cy[4] = {3, 6, 9, 12}, cz[4] = {1, 4, 7, 10};
 #pragma unroll
   for (int m = 1; m <= 4; ++m) {
     const float4 u = ld4<ST>(box, e - m * BX);
     const float4 d = ld4<ST>(box, e + m * BX);
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      s[j] = fmaf(c[cy[m - 1]], comp(u, j) + comp(d, j), s[j]);
+    const f32x2 k = cc(cy[m - 1]);
+    s0 = fma2(k, add2(pk2(u.x, u.y), pk2(d.x, d.y)), s0);
+    s1 = fma2(k, add2(pk2(u.z, u.w), pk2(d.z, d.w)), s1);
   }
 #pragma unroll
-  for (int m = 1; m <= 4; ++m)
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      s[j] = fmaf(c[cz[m - 1]], comp(q[4 - m], j) + comp(q[4 + m], j), s[j]);
-  return make_float4(s[0], s[1], s[2], s[3]);
+  for (int m = 1; m <= 4; ++m) {
+    const float4 &u = q[4 - m], &d = q[4 + m];
+    const f32x2 k = cc(cz[m - 1]);
+    s0 = fma2(k, add2(pk2(u.x, u.y), pk2(d.x, d.y)), s0);
+    s1 = fma2(k, add2(pk2(u.z, u.w), pk2(d.z, d.w)), s1);
+  }
+  const float2 a = upk2(s0), b = upk2(s1);
+  return make_float4(a.x, a.y, b.x, b.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -711,36 +791,45 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
       const float bz = ez < kNBound ? s_bound[ez] : 1.0f;  // ez >= 0 here
       float bj[4];
 #pragma unroll
-      for (int jj = 0; jj < 4; ++jj) {
-        const float b = fminf(bxy[jj], bz);
-        bj[jj] = b;
+      for (int jj = 0; jj < 4; ++jj) bj[jj] = fminf(bxy[jj], bz);
+      // leapfrog and taper per pair of cells (x, x+1), (x+2, x+3); each lane
+      // rounds as the scalar operation of cpu_prop.cc:233-248 and
+      // cpu_prop.cc:150-160 does.  Products are scalar in the reference
+      // order (a packed product feeding a packed add would be contracted).
+      auto mulx = [](f32x2 a, f32x2 b) {
+        if constexpr (FUSED) return mul2(a, b);
+        else return mul2s(a, b);
+      };
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const f32x2 b = pk2(bj[2 * h], bj[2 * h + 1]);
         if (M::kBoxA) {
-          float old = comp(oa, jj);
-          if (M::kDampA) old = __fmul_rn(old, b);
-          float v = FUSED ? fmaf(comp(va, jj), comp(ga, jj),
-                                 comp(ca, jj) + comp(ca, jj) - old)
-                       : leapfrog(comp(va, jj), comp(ga, jj), comp(ca, jj),
-                                  old);
+          f32x2 old = cells2(oa, h);
+          if (M::kDampA) old = mulx(old, b);
+          const f32x2 c = cells2(ca, h);
+          f32x2 v = FUSED ? fma2(cells2(va, h), cells2(ga, h),
+                                 sub2(add2(c, c), old))
+                          : leapfrog2(cells2(va, h), cells2(ga, h), c, old);
           // the adjoint of the linearised step injects its data before the
           // taper (see below); every other tapered mode tapers here
-          if (MODE != kModeBornAdj && M::kDampA) v = __fmul_rn(v, b);
-          set_comp(na, jj, v);
+          if (MODE != kModeBornAdj && M::kDampA) v = mulx(v, b);
+          set_cells2(na, h, v);
         } else if (MODE == kModeAdjoint) {
           // receiver level not propagated (it == 0): both damping passes
-          set_comp(na, jj, __fmul_rn(__fmul_rn(comp(oa, jj), b), b));
+          set_cells2(na, h, mulx(mulx(cells2(oa, h), b), b));
         }
         if (M::kBoxB) {
-          float old = comp(ob, jj);
-          if (M::kDampB) old = __fmul_rn(old, b);
-          float v = FUSED ? fmaf(comp(vb, jj), comp(sb, jj),
-                                 comp(cb, jj) + comp(cb, jj) - old)
-                       : leapfrog(comp(vb, jj), comp(sb, jj), comp(cb, jj),
-                                  old);
+          f32x2 old = cells2(ob, h);
+          if (M::kDampB) old = mulx(old, b);
+          const f32x2 c = cells2(cb, h);
+          f32x2 v = FUSED ? fma2(cells2(vb, h), cells2(sb, h),
+                                 sub2(add2(c, c), old))
+                          : leapfrog2(cells2(vb, h), cells2(sb, h), c, old);
           // linearised Born: scattering source m (A s) inside the taper
           if (MODE == kModeBornLin)
-            v = __fadd_rn(v, __fmul_rn(comp(im, jj), comp(ga, jj)));
-          if (M::kDampB) v = __fmul_rn(v, b);
-          set_comp(nb, jj, v);
+            v = add2(v, mulx(cells2(im, h), cells2(ga, h)));
+          if (M::kDampB) v = mulx(v, b);
+          set_cells2(nb, h, v);
         }
       }
 
@@ -784,11 +873,11 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
           if (MODE == kModeForward) {
             // Born coupling r += 1e-6 s img, then extraction from r
 #pragma unroll
-            for (int jj = 0; jj < 4; ++jj)
-              set_comp(nb, jj,
-                       __fadd_rn(comp(nb, jj),
-                                 __fmul_rn(__fmul_rn(1e-6f, comp(na, jj)),
-                                           comp(im, jj))));
+            for (int h = 0; h < 2; ++h)
+              set_cells2(nb, h,
+                        add2(cells2(nb, h),
+                             mulx(mulx(pk2(1e-6f, 1e-6f), cells2(na, h)),
+                                  cells2(im, h))));
           }
           if (MODE == kModeForward || MODE == kModeBornLin) {
             if (p.pb.active) extract_row(p.pb, n1, n2, zo, gy, gx, nb);
@@ -797,10 +886,10 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
           } else if (MODE == kModeAdjoint) {
             // s is the new level when propagated, else the stored one
             float4 ni;
-            ni.x = __fadd_rn(im.x, __fmul_rn(nb.x, na.x));
-            ni.y = __fadd_rn(im.y, __fmul_rn(nb.y, na.y));
-            ni.z = __fadd_rn(im.z, __fmul_rn(nb.z, na.z));
-            ni.w = __fadd_rn(im.w, __fmul_rn(nb.w, na.w));
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+              set_cells2(ni, h, add2(cells2(im, h),
+                                    mulx(cells2(nb, h), cells2(na, h))));
             st4(p.img_out + idx, ni);
             store_a(na);
             if (PB) store_b(nb);
