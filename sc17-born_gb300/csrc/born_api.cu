@@ -358,7 +358,7 @@ int launch(born_handle *h, int mode, bool pa, bool pb, const void *a_cur,
 int check_device_error(born_handle *h);
 
 // Autotuner: times every tile configuration of one step mode on the
-// current grid (two sweeps of one warm-up and four timed launches, CUDA
+// current grid (three sweeps of two warm-up and eight timed launches, CUDA
 // events on the handle's stream) and keeps the fastest, per storage type.  It runs on the
 // scratch levels f0/f1/r0/r1 and a temporary image with every point set
 // inactive, so it never touches the source levels kept for rtm_adjoint nor
@@ -388,12 +388,13 @@ int tune_mode(born_handle *h, int mode) {
     const void *reset[] = {h->f0, h->f1, h->r0, h->r1};
     rc = born_lp_prologue(h, h->stream, reset, 4);
   }
-  // two interleaved sweeps over the tiles, one warm-up and four timed
-  // launches each, best time per tile: a single short timing is noisy
-  // enough to pick a tile 5-7 % slower than the best
+  // interleaved sweeps over the tiles, best sweep average per tile: tiles
+  // 3-4 % apart in the time loop were confused by two sweeps of four timed
+  // launches (about 1.3 ms each on a 368^3 grid)
+  constexpr int kSweeps = 3, kWarm = 2, kTimed = 8;
   const int ncfg = born::tile_cfg_count();
   std::vector<float> cfg_ms(ncfg, -1.f);
-  for (int sweep = 0; sweep < 2 * ncfg && !rc; ++sweep) {
+  for (int sweep = 0; sweep < kSweeps * ncfg && !rc; ++sweep) {
     const int cfg = sweep % ncfg;
     h->tile_cfg = cfg;
     StepParams p;
@@ -409,15 +410,15 @@ int tune_mode(born_handle *h, int mode) {
     }
     const void *cen[born::kNumCentre] = {h->f1, h->r1, h->vel2, h->vel1,
                                          mode == kModeForward ? h->refl : timg};
-    for (int it = 0; it < 5 && !rc; ++it) {
-      if (it == 1) cudaEventRecord(e0, h->stream);
+    for (int it = 0; it < kWarm + kTimed && !rc; ++it) {
+      if (it == kWarm) cudaEventRecord(e0, h->stream);
       rc = launch(h, mode, true, pb, h->f0, h->r0, cen, p);
     }
     cudaEventRecord(e1, h->stream);
     cudaEventSynchronize(e1);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
-    ms /= 4.f;
+    ms /= (float)kTimed;
     if (!rc && (cfg_ms[cfg] < 0.f || ms < cfg_ms[cfg])) cfg_ms[cfg] = ms;
   }
   for (int cfg = 0; cfg < ncfg; ++cfg)
@@ -444,6 +445,79 @@ int ensure_tuned(born_handle *h, int mode) {
     return BORN_OK;
   return tune_mode(h, mode);
 }
+
+// Refines a mode's tile choice on the first steps of a long time loop.  Every
+// tile gives bit-identical results, so the loop's own steps are timed: CUDA
+// events around groups of kLoopGroup consecutive steps, the tiles in turn,
+// kLoopRounds times, from the loop's second step (the adjoint's first step
+// is a lighter variant); the loop then goes on with the fastest tile, kept
+// for later loops of the same storage and mode.  The scratch tuner's
+// launches differ from a loop's (inactive points, fixed buffers) and picked
+// a forward tile that ran 3.4 % slower in the loop than the best one
+// (368^3 grid).
+constexpr int kLoopGroup = 8, kLoopRounds = 2, kLoopMinSteps = 400;
+
+class LoopTuner {
+ public:
+  LoopTuner(born_handle *h, int mode, int nsteps) : h_(h), mode_(mode) {
+    if (!h->autotune || h->tile_cfg >= 0 || nsteps < kLoopMinSteps ||
+        h->loop_tuned[h->storage][mode])
+      return;
+    ncfg_ = born::tile_cfg_count();
+    groups_ = ncfg_ * kLoopRounds;
+    ev_.assign(groups_ + 1, nullptr);
+    for (cudaEvent_t &e : ev_)
+      if (cudaEventCreate(&e) != cudaSuccess) {
+        release();
+        return;
+      }
+    on_ = true;
+  }
+  ~LoopTuner() { release(); }
+  LoopTuner(const LoopTuner &) = delete;
+  LoopTuner &operator=(const LoopTuner &) = delete;
+
+  // before launching the loop's step k (k = 0 for its first step)
+  int before(int k) {
+    if (!on_ || k < 1 || (k - 1) % kLoopGroup != 0) return BORN_OK;
+    const int g = (k - 1) / kLoopGroup;
+    if (g > groups_) return BORN_OK;
+    CK(h_, cudaEventRecord(ev_[g], h_->stream));
+    if (g < groups_) {
+      h_->tuned_cfg[h_->storage][mode_] = g % ncfg_;
+      return BORN_OK;
+    }
+    CK(h_, cudaEventSynchronize(ev_[groups_]));
+    std::vector<float> best(ncfg_, -1.f);
+    for (int i = 0; i < groups_; ++i) {
+      float ms = 0.f;
+      CK(h_, cudaEventElapsedTime(&ms, ev_[i], ev_[i + 1]));
+      float &b = best[i % ncfg_];
+      if (b < 0.f || ms < b) b = ms;
+    }
+    int pick = 0;
+    for (int c = 1; c < ncfg_; ++c)
+      if (best[c] < best[pick]) pick = c;
+    h_->tuned_cfg[h_->storage][mode_] = pick;
+    h_->tuned_ms[h_->storage][mode_] = best[pick] / kLoopGroup;
+    h_->loop_tuned[h_->storage][mode_] = true;
+    release();
+    return BORN_OK;
+  }
+
+ private:
+  void release() {
+    for (cudaEvent_t e : ev_)
+      if (e) cudaEventDestroy(e);
+    ev_.clear();
+    on_ = false;
+  }
+  born_handle *h_;
+  int mode_;
+  int ncfg_ = 0, groups_ = 0;
+  bool on_ = false;
+  std::vector<cudaEvent_t> ev_;
+};
 
 // Every this many steps the loops look at the device error word, so that a
 // kernel whose bounded wait gave up stops the loop instead of being followed
@@ -689,6 +763,7 @@ int born_create_space(born_handle *h, float d1, float d2, float d3, float bc_a,
   CK(h, cudaStreamSynchronize(h->stream));
   h->have_space = true;
   h->generation++;
+  h->reset_tuning();  // tile choices are per grid
   return BORN_OK;
 }
 
@@ -774,7 +849,10 @@ int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
   }
   float *p0 = h->s0, *p1 = h->s1;
   const float scale = 1 / (float)jts;
+  LoopTuner tuner(h, kModeSource, nt + 1);
   for (int it = 0; it <= nt; ++it) {
+    rc = tuner.before(it);
+    if (rc) return rc;
     const int id = it / h->jt_s, ii = it - id * h->jt_s;
     StepParams p;
     base_params(h, p);
@@ -835,7 +913,10 @@ int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap,
   float *rp0 = h->r0, *rp1 = h->r1;
   const float scale = -1 / (float)h->jt;
   PointSet pending = point_view(h->src, 0, 0, h->tab_s, 0.f, false);
+  LoopTuner tuner(h, kModeAdjoint, nt);
   for (int it = nt - 1; it >= 0; --it) {
+    rc = tuner.before(nt - 1 - it);
+    if (rc) return rc;
     const int id_s = (it + 1) / h->jt_s, i_s = it + 1 - id_s * h->jt_s;
     const int id = it / h->jt_d, ii = it - id * h->jt_d;
     const bool pa = it > 0, pb = it < nt - 1;
@@ -902,7 +983,10 @@ int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out) {
   }
   float *sp0 = h->f0, *sp1 = h->f1, *rp0 = h->r0, *rp1 = h->r1;
   const float scale = 1 / (float)jt;
+  LoopTuner tuner(h, kModeForward, nt);
   for (int it = 0; it < nt; ++it) {
+    rc = tuner.before(it);
+    if (rc) return rc;
     const int id = it / jt, ii = it - id * jt;
     StepParams p;
     base_params(h, p);
@@ -1207,8 +1291,7 @@ int born_autotune(born_handle *h, int enable) {
   int rc = check_ready(h);
   if (rc) return rc;
   h->autotune = enable != 0;
-  for (int st = 0; st < 3; ++st)
-    for (int m = 0; m < 6; ++m) h->tuned_cfg[st][m] = -1;
+  h->reset_tuning();
   if (!enable) return BORN_OK;
   const int modes[] = {kModeSource, kModeForward, kModeAdjoint,
                        born::kModeModel, born::kModeBornLin,

@@ -85,6 +85,17 @@ struct born_handle {
                          {-1, -1, -1, -1, -1, -1},
                          {-1, -1, -1, -1, -1, -1}};
   float tuned_ms[4][6] = {};
+  // tile choice refined on a time loop's own steps (LoopTuner in
+  // born_api.cu), per storage and step mode
+  bool loop_tuned[4][6] = {};
+  void reset_tuning() {
+    for (int st = 0; st < 4; ++st)
+      for (int m = 0; m < 6; ++m) {
+        tuned_cfg[st][m] = -1;
+        tuned_ms[st][m] = 0.f;
+        loop_tuned[st][m] = false;
+      }
+  }
   // wavefield level storage (born::Storage) and, for 16-bit storage, the
   // level records [kNumLevelBufs][2 slots][2 words], the number of writes of
   // each level buffer since its last reset (its record slot is the parity)
