@@ -134,6 +134,12 @@ struct StepParams {
 constexpr unsigned int kErrWaitTimeout = 1u;
 constexpr int kZStages = 3;  // z-window ring depth (new planes, 2 ahead)
 constexpr int kOStages = 3;  // output ring depth (output planes, 2 ahead)
+// output ring depth of a mode (at most kOStages): the forward step keeps two
+// stages so that a 64x8 tile fits four CTAs per SM (shared memory) instead
+// of three
+constexpr int out_stages(int mode) {
+  return mode == kModeForward ? 2 : kOStages;
+}
 
 struct StepMaps {
   CUtensorMap box_a, box_b;       // halo boxes of the current levels

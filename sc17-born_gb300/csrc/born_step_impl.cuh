@@ -548,8 +548,9 @@ struct Layout {
   static constexpr uint32_t kZTx = M::kNF * T::kZRaw;
   static constexpr uint32_t kOTx =
       M::kNF * T::kBoxRaw + centre_bytes<MODE, M::kMask, T>(true);
+  static constexpr int kOSt = out_stages(MODE);  // output ring depth
   static constexpr size_t kSmem =
-      (size_t)kZStages * kZStage + (size_t)kOStages * kOStage + 128;
+      (size_t)kZStages * kZStage + (size_t)kOSt * kOStage + 128;
 };
 
 // Scales of one step's levels (16-bit storage), shared by the CTA.
@@ -574,7 +575,7 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   constexpr int BX = T::kBX;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t zbars[kZStages];
-  __shared__ __align__(8) uint64_t obars[kOStages];
+  __shared__ __align__(8) uint64_t obars[kOStages];  // the first LY::kOSt
   __shared__ int abort_flag;
   __shared__ float s_bound[kNBound];
   __shared__ StepScales s_sc;
@@ -612,7 +613,7 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
 
   if (tid == 0) {
     for (int s = 0; s < kZStages; ++s) mbar_init(&zbars[s], 1);
-    for (int s = 0; s < kOStages; ++s) mbar_init(&obars[s], 1);
+    for (int s = 0; s < LY::kOSt; ++s) mbar_init(&obars[s], 1);
     // a wait elsewhere already gave up: the whole CTA leaves untouched
     abort_flag = *reinterpret_cast<volatile unsigned int *>(p.err) != 0u;
     mbar_fence_init();
@@ -675,7 +676,7 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   };
   auto issue_out = [&](int j) {
     const int plane = z0 + j;
-    const int st = j % kOStages;
+    const int st = j % LY::kOSt;
     mbar_expect_tx(&obars[st], LY::kOTx);
     unsigned char *dst = oring + st * LY::kOStage;
     if (M::kBoxA)
@@ -695,7 +696,7 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   if (tid == 0) {
     if (NF > 0)
       for (int k = 0; k < min(K, kZStages); ++k) issue_z(k);
-    for (int j = 0; j < min(J, kOStages); ++j) issue_out(j);
+    for (int j = 0; j < min(J, LY::kOSt); ++j) issue_out(j);
   }
 
   float4 qa[9], qb[9];
@@ -735,8 +736,8 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
     }
 
     if (j >= 0 && ok) {
-      const int os = j % kOStages;
-      ok = mbar_wait_bounded(&obars[os], (uint32_t)((j / kOStages) & 1));
+      const int os = j % LY::kOSt;
+      ok = mbar_wait_bounded(&obars[os], (uint32_t)((j / LY::kOSt) & 1));
       const unsigned char *ost = oring + os * LY::kOStage;
       const unsigned char *cst = ost + NF * T::kBoxBytes;
       auto centre = [&](int slot) {
@@ -913,13 +914,13 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
     if (tid == 0) {
       fence_proxy_async();
       if (NF > 0 && k + kZStages < K) issue_z(k + kZStages);
-      if (j >= 0 && j + kOStages < J) issue_out(j + kOStages);
+      if (j >= 0 && j + LY::kOSt < J) issue_out(j + LY::kOSt);
     }
   }
 
   if (abort_flag && tid == 0) {
     // drain whatever is still in flight (bounded) before the CTA retires
-    for (int s = 0; s < kZStages + kOStages; ++s) {
+    for (int s = 0; s < kZStages + LY::kOSt; ++s) {
       uint64_t *b = s < kZStages ? &zbars[s] : &obars[s - kZStages];
       const uint64_t t0 = global_ns();
       while (!mbar_try_wait(b, 0) && !mbar_try_wait(b, 1) &&
