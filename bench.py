@@ -329,10 +329,12 @@ def run_gpu_arm(args):
         prop.synchronize()
         torch.cuda.synchronize()
     launches = prop.launches - launches0
-    tiles = {}
+    tiles, tile_ms = {}, {}
     for mode, name in ((1, "forward"), (0, "source"), (2, "adjoint")):
         cfg, ms = prop.tuned_config(mode)
         tiles[name] = cfg
+        # per-tile ms per launch as the loop's own refinement measured them
+        tile_ms[name] = [round(v, 4) for v in prop.loop_tile_ms(mode)]
     t_ms = start.elapsed_time(stop)
     t_ms = barrier_max(t_ms, world)
     fwd_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
@@ -413,6 +415,7 @@ def run_gpu_arm(args):
                        (", image summed over the ranks every step (NCCL "
                         "all-reduce)" if world > 1 else "")},
             "roofline": roofline, "phases": phases, "tile_cfg": tiles,
+            "tile_ms_per_launch": tile_ms,
             "clocks": clk.summary(), "gpu_launches": launches,
             "e2e": e2e, "cpu_baseline": cpu, "fused_fma": fused,
         }

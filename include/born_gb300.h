@@ -305,6 +305,11 @@ int born_autotune(born_handle *h, int enable);
  * tuner's time per launch. */
 int born_tuned_config(const born_handle *h, int mode, int *cfg,
                       float *ms_per_launch);
+/* Time loops of 400 steps or more refine a mode's tile on their own steps
+ * (every tile gives the same results): ms[c] receives the time per launch
+ * the last refinement of the mode measured for tile configuration c (0 when
+ * not measured), for c < n, under the current storage. */
+int born_loop_tile_ms(const born_handle *h, int mode, float *ms, int n);
 /* Kernels launched on this handle since creation (for accounting). */
 long long born_kernel_launches(const born_handle *h);
 

@@ -91,6 +91,7 @@ _SIGS = {
     "born_get_storage": (C.c_int, [_vp]),
     "born_autotune": (C.c_int, [_vp, C.c_int]),
     "born_tuned_config": (C.c_int, [_vp, C.c_int, _ip, _fp]),
+    "born_loop_tile_ms": (C.c_int, [_vp, C.c_int, _fp, C.c_int]),
     "born_kernel_launches": (C.c_longlong, [_vp]),
     "born_stream": (_vp, [_vp]),
     # batched shots (include/born_gb300.h section 4)
@@ -267,6 +268,14 @@ class Handle:
         self.check(self.lib.born_tuned_config(self.h, mode, C.byref(cfg),
                                               C.byref(ms)))
         return cfg.value, ms.value
+
+    def loop_tile_ms(self, mode: int):
+        """ms per launch of every tile configuration as the last in-loop
+        refinement of `mode` measured it (0.0: not measured)."""
+        n = int(self.lib.born_tile_config_count())
+        out = (C.c_float * n)()
+        self.check(self.lib.born_loop_tile_ms(self.h, mode, out, n))
+        return [float(v) for v in out]
 
     def synchronize(self):
         self.check(self.lib.born_synchronize(self.h))

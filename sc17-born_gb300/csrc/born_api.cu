@@ -447,15 +447,16 @@ int ensure_tuned(born_handle *h, int mode) {
 }
 
 // Refines a mode's tile choice on the first steps of a long time loop.  Every
-// tile gives bit-identical results, so the loop's own steps are timed: CUDA
-// events around groups of kLoopGroup consecutive steps, the tiles in turn,
-// kLoopRounds times, from the loop's second step (the adjoint's first step
-// is a lighter variant); the loop then goes on with the fastest tile, kept
-// for later loops of the same storage and mode.  The scratch tuner's
-// launches differ from a loop's (inactive points, fixed buffers) and picked
-// a forward tile that ran 3.4 % slower in the loop than the best one
-// (368^3 grid).
-constexpr int kLoopGroup = 8, kLoopRounds = 2, kLoopMinSteps = 400;
+// tile gives bit-identical results, so the loop's own steps are timed: from
+// the loop's second step (the adjoint's first step is a lighter variant),
+// the tiles take turns in groups of one untimed step (the first launch with
+// a tile pays for its descriptors and attributes on the host) and
+// kLoopGroup timed ones between CUDA events, kLoopRounds times; the loop
+// then goes on with the tile of the smallest group time, kept for later
+// loops of the same storage and mode.  The scratch tuner's launches differ
+// from a loop's (inactive points, fixed buffers) and picked a forward tile
+// that ran 3.4 % slower in the loop than the best one (368^3 grid).
+constexpr int kLoopGroup = 8, kLoopRounds = 3, kLoopMinSteps = 400;
 
 class LoopTuner {
  public:
@@ -463,9 +464,10 @@ class LoopTuner {
     if (!h->autotune || h->tile_cfg >= 0 || nsteps < kLoopMinSteps ||
         h->loop_tuned[h->storage][mode])
       return;
-    ncfg_ = born::tile_cfg_count();
+    ncfg_ = std::min(born::tile_cfg_count(), born_handle::kMaxTileCfgs);
     groups_ = ncfg_ * kLoopRounds;
-    ev_.assign(groups_ + 1, nullptr);
+    if (1 + groups_ * (kLoopGroup + 1) >= nsteps) return;
+    ev_.assign(2 * groups_, nullptr);
     for (cudaEvent_t &e : ev_)
       if (cudaEventCreate(&e) != cudaSuccess) {
         release();
@@ -479,25 +481,29 @@ class LoopTuner {
 
   // before launching the loop's step k (k = 0 for its first step)
   int before(int k) {
-    if (!on_ || k < 1 || (k - 1) % kLoopGroup != 0) return BORN_OK;
-    const int g = (k - 1) / kLoopGroup;
-    if (g > groups_) return BORN_OK;
-    CK(h_, cudaEventRecord(ev_[g], h_->stream));
+    if (!on_ || k < 1) return BORN_OK;
+    const int g = (k - 1) / (kLoopGroup + 1), r = (k - 1) % (kLoopGroup + 1);
+    if (r == 1 && g < groups_)  // the group's timed steps start here
+      CK(h_, cudaEventRecord(ev_[2 * g], h_->stream));
+    if (r != 0) return BORN_OK;
+    if (g > 0) CK(h_, cudaEventRecord(ev_[2 * g - 1], h_->stream));
     if (g < groups_) {
       h_->tuned_cfg[h_->storage][mode_] = g % ncfg_;
       return BORN_OK;
     }
-    CK(h_, cudaEventSynchronize(ev_[groups_]));
+    CK(h_, cudaEventSynchronize(ev_[2 * groups_ - 1]));
     std::vector<float> best(ncfg_, -1.f);
     for (int i = 0; i < groups_; ++i) {
       float ms = 0.f;
-      CK(h_, cudaEventElapsedTime(&ms, ev_[i], ev_[i + 1]));
+      CK(h_, cudaEventElapsedTime(&ms, ev_[2 * i], ev_[2 * i + 1]));
       float &b = best[i % ncfg_];
       if (b < 0.f || ms < b) b = ms;
     }
     int pick = 0;
     for (int c = 1; c < ncfg_; ++c)
       if (best[c] < best[pick]) pick = c;
+    for (int c = 0; c < ncfg_; ++c)
+      h_->loop_ms[h_->storage][mode_][c] = best[c] / kLoopGroup;
     h_->tuned_cfg[h_->storage][mode_] = pick;
     h_->tuned_ms[h_->storage][mode_] = best[pick] / kLoopGroup;
     h_->loop_tuned[h_->storage][mode_] = true;
@@ -1310,6 +1316,14 @@ int born_tuned_config(const born_handle *h, int mode, int *cfg,
   if (cfg)
     *cfg = h->tile_cfg >= 0 ? h->tile_cfg : h->tuned_cfg[h->storage][mode];
   if (ms_per_launch) *ms_per_launch = h->tuned_ms[h->storage][mode];
+  return BORN_OK;
+}
+
+int born_loop_tile_ms(const born_handle *h, int mode, float *ms, int n) {
+  if (!h || mode < 0 || mode > 5 || !ms || n < 0) return BORN_EINVAL;
+  for (int c = 0; c < n; ++c)
+    ms[c] = c < born_handle::kMaxTileCfgs ? h->loop_ms[h->storage][mode][c]
+                                          : 0.f;
   return BORN_OK;
 }
 

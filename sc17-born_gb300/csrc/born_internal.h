@@ -88,12 +88,17 @@ struct born_handle {
   // tile choice refined on a time loop's own steps (LoopTuner in
   // born_api.cu), per storage and step mode
   bool loop_tuned[4][6] = {};
+  // ms per launch of every tile as the last refinement measured it (0: not
+  // measured)
+  static constexpr int kMaxTileCfgs = 8;
+  float loop_ms[4][6][kMaxTileCfgs] = {};
   void reset_tuning() {
     for (int st = 0; st < 4; ++st)
       for (int m = 0; m < 6; ++m) {
         tuned_cfg[st][m] = -1;
         tuned_ms[st][m] = 0.f;
         loop_tuned[st][m] = false;
+        for (int c = 0; c < kMaxTileCfgs; ++c) loop_ms[st][m][c] = 0.f;
       }
   }
   // wavefield level storage (born::Storage) and, for 16-bit storage, the

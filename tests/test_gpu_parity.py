@@ -176,3 +176,19 @@ def test_device_image_view_and_single_rank_stack(gpu, po):
     assert np.array_equal(t.cpu().numpy(), got["image"])
     # without a process group the stack is the image itself
     assert np.array_equal(gpu.stack_image(prop).cpu().numpy(), got["image"])
+
+
+def test_loop_tile_refinement_keeps_parity(gpu, po):
+    """A loop of 400 steps or more switches tiles while it times its own
+    steps; results stay bit-identical and each mode keeps the tile with the
+    smallest measured time."""
+    c = cases.make_case(41, shape=(40, 44, 56), nt=420, jt=1,
+                        sinc=po.sinc_table)
+    prop = gpu.Gb300Prop()
+    got = po.run_case(prop, c)
+    check(got, po.run_case(po.PortProp(), c))
+    for mode in (0, 1, 2):  # source, forward, adjoint
+        ms = prop.loop_tile_ms(mode)
+        assert all(v > 0 for v in ms), (mode, ms)
+        cfg, _ = prop.tuned_config(mode)
+        assert ms[cfg] == min(ms), (mode, cfg, ms)
