@@ -8,18 +8,25 @@
 //   * z ring (kZStages): the TX x TY centre tile of every propagated field's
 //     current level for each new plane; its values enter the 9-plane z window
 //     kept in registers;
-//   * output ring (kOStages): for the plane being written, the
+//   * output ring (out_stages(mode) deep): for the plane being written, the
 //     (TX+8) x (TY+8) halo box of every propagated field (x/y neighbours) and
 //     the per-cell inputs (previous levels, velocities, image or
 //     reflectivity), one TX x TY tile each.
 // A plane's centre is thus read twice (z ring, then inside its box four
 // planes later, from L2), which keeps the shared memory per CTA small enough
-// for three 128-thread CTAs per SM.
+// for three 128-thread CTAs per SM (four for the forward step, whose ring
+// is two stages deep).
+// The stencil's neighbour sums and running sums, the leapfrog and the
+// imaging adds run on packed FP32 pairs (add/sub.rn.f32x2: two cells per
+// instruction, each lane rounded like the scalar form); the products of the
+// reference-order arithmetic stay scalar mul.rn (see f32x2 in
+// born_step_impl.cuh).
 // The new level (and the image) are written once with float4 stores, so HBM
 // sees the compulsory bytes only.
 //
 // Reference semantics fused into the pass (base/cpu_prop.cc):
 //   prop (224-253)       stencil, same left-to-right sum, no FMA contraction
+//                        (bit-identical, also in the packed pairs)
 //   damp (141-165)       the new level is scaled by b(edge); the scaling that
 //                        the reference applies in place to the current level
 //                        is applied when that level is read back as "old"
@@ -133,7 +140,7 @@ struct StepParams {
 
 constexpr unsigned int kErrWaitTimeout = 1u;
 constexpr int kZStages = 3;  // z-window ring depth (new planes, 2 ahead)
-constexpr int kOStages = 3;  // output ring depth (output planes, 2 ahead)
+constexpr int kOStages = 3;  // largest output ring depth (planes 2 ahead)
 // output ring depth of a mode (at most kOStages): the forward step keeps two
 // stages so that a 64x8 tile fits four CTAs per SM (shared memory) instead
 // of three
