@@ -377,6 +377,11 @@ def run_gpu_arm(args):
                 "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": BYTES_PER_CELL["adjoint"] * n_int,
                 "avg_launch_ms": round(adj_launch_ms, 4)}
+    # second denominator: what plain streaming sustains for the adjoint
+    # step's own mix of arrays (7 read, 3 written, one grid field each)
+    mix = born.stream_mix_gbs(7, 3, nx * ny * nz)
+    roofline["stream_mix"] = {"reads": 7, "writes": 3, "gbs": round(mix, 1),
+                              "frac": round(achieved / mix, 4)}
     phases = {"forward_ms": round(fwd_ms, 2), "source_ms": round(src_ms, 2),
               "adjoint_ms": round(adj_ms, 2),
               "forward_GBps": round(BYTES_PER_CELL["forward"] * n_int * nt /

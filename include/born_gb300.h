@@ -291,6 +291,16 @@ int born_batch_synchronize(born_batch *b);
 int born_dot_f64_noalloc(const float *a, const float *b, long long n,
                          double *out, void *stream);
 
+/* Measurement: the bandwidth (GB/s, read + write bytes) that plain float4
+ * loads and stores sustain over `reads` input and `writes` output arrays of
+ * n floats each (1 <= reads <= 8, 1 <= writes <= 4, n a multiple of 4), on
+ * the current device: the streaming ceiling of a step kernel's mix of arrays
+ * (RTM adjoint 7 + 3, Born forward 6 + 2, source propagation 3 + 1).  No
+ * reference counterpart.  Allocates and frees (reads + writes) * n floats;
+ * best of two grid sizes, `reps` timed launches each. */
+int born_stream_mix_gbs(int reads, int writes, long long n, int reps,
+                        float *gbs);
+
 /* Tuning: tile configuration index (0..born_tile_config_count()-1, or -1 for
  * the built-in choice) and z-segment depth (0 = automatic). */
 int born_tile_config_count(void);

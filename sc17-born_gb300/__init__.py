@@ -92,6 +92,8 @@ _SIGS = {
     "born_autotune": (C.c_int, [_vp, C.c_int]),
     "born_tuned_config": (C.c_int, [_vp, C.c_int, _ip, _fp]),
     "born_loop_tile_ms": (C.c_int, [_vp, C.c_int, _fp, C.c_int]),
+    "born_stream_mix_gbs": (C.c_int, [C.c_int, C.c_int, C.c_longlong,
+                                      C.c_int, _fp]),
     "born_kernel_launches": (C.c_longlong, [_vp]),
     "born_stream": (_vp, [_vp]),
     # batched shots (include/born_gb300.h section 4)
@@ -453,6 +455,17 @@ class Gb300Prop(Handle):
 
 # ---------------------------------------------------------------------------
 # Stacking images across ranks
+
+def stream_mix_gbs(reads: int, writes: int, n: int, reps: int = 20) -> float:
+    """GB/s that plain float4 streaming sustains over `reads` input and
+    `writes` output arrays of n floats on the current device (the ceiling of
+    a step kernel's mix of arrays)."""
+    out = C.c_float()
+    rc = lib().born_stream_mix_gbs(reads, writes, n, reps, C.byref(out))
+    if rc != BORN_OK:
+        raise BornError(rc, "born_stream_mix_gbs failed")
+    return out.value
+
 
 def stack_tensor(t, group=None):
     """Sums a tensor over the ranks of ``torch.distributed`` in place (NCCL

@@ -49,6 +49,15 @@ def test_no_device_gives_enodev_not_exit(born):
     assert born.lib().born_default_status() == -6
 
 
+def test_stream_mix_rejects_bad_arguments(born):
+    """Argument checks come before any CUDA call."""
+    L, out = born.lib(), C.c_float()
+    for args in ((0, 1, 16, 1), (9, 1, 16, 1), (1, 0, 16, 1), (1, 5, 16, 1),
+                 (1, 1, 6, 1), (1, 1, 0, 1), (1, 1, 16, 0)):
+        assert L.born_stream_mix_gbs(*args, C.byref(out)) == -1, args
+    assert L.born_stream_mix_gbs(1, 1, 16, 1, None) == -1
+
+
 def test_sinc_tables_match_oracle(born, po):
     for n in (1, 2, 3, 4, 5, 8, 16):
         assert np.array_equal(born.sinc_table(n), po.sinc_table(n)), n

@@ -192,3 +192,13 @@ def test_loop_tile_refinement_keeps_parity(gpu, po):
         assert all(v > 0 for v in ms), (mode, ms)
         cfg, _ = prop.tuned_config(mode)
         assert ms[cfg] == min(ms), (mode, cfg, ms)
+
+
+def test_stream_mix_ceiling_measures(gpu):
+    """The streaming-ceiling probe runs and gives a plausible HBM rate for a
+    mix larger than L2 (2 x 64 MiB for a copy, 10 x 64 MiB for the
+    adjoint's mix)."""
+    n = 1 << 24
+    for r, w in ((1, 1), (7, 3)):
+        gbs = gpu.stream_mix_gbs(r, w, n, reps=3)
+        assert 500.0 < gbs < 20000.0, (r, w, gbs)
