@@ -10,7 +10,12 @@ the RTM adjoint (sourceProp + rtmAdjoint) of configuration c2 (256^3 model,
          copies inside the timed region, in the call order of
          rtm_zero_op_3d.cc
   roofline  achieved GB/s of the dominant kernel (the fused RTM adjoint
-         step) against the measured HBM copy bandwidth
+         step) against the measured HBM copy bandwidth, and (stream_mix)
+         against what plain streaming sustains for the step's own 7 read
+         and 3 written arrays
+  tile_ms_per_launch  per-tile time per launch of each step as the time
+         loops measured them on their own steps (the chosen tile in
+         tile_cfg)
   cpu_baseline  the oracle (C restatement of the reference cpuProp) on the
          host cores, on a bounded sample of the same workload
 
