@@ -13,6 +13,8 @@ the RTM adjoint (sourceProp + rtmAdjoint) of configuration c2 (256^3 model,
          step) against the measured HBM copy bandwidth, and (stream_mix)
          against what plain streaming sustains for the step's own 7 read
          and 3 written arrays
+  shot_steps_per_s  time steps of whole shots (Born forward + RTM adjoint)
+         per second, over all ranks
   tile_ms_per_launch  per-tile time per launch of each step as the time
          loops measured them on their own steps (the chosen tile in
          tile_cfg)
@@ -424,6 +426,10 @@ def run_gpu_arm(args):
                        "parallelism": f"shots x{world} (one per GPU)" +
                        (", image summed over the ranks every step (NCCL "
                         "all-reduce)" if world > 1 else "")},
+            # one shot-step: a time step of one shot's Born forward + RTM
+            # adjoint (source propagation included), over all ranks
+            "shot_steps_per_s": round(world * nt * args.steps / (t_ms / 1e3),
+                                      1),
             "roofline": roofline, "phases": phases, "tile_cfg": tiles,
             "tile_ms_per_launch": tile_ms,
             "clocks": clk.summary(), "gpu_launches": launches,
