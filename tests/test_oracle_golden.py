@@ -1,6 +1,7 @@
 """The oracle (C restatement of base/cpu_prop.cc) against the golden
 fixtures made by running the reference's own compiled CPU path, and directly
 against that compiled path where the reference sources are present."""
+import ctypes as C
 import glob
 import os
 
@@ -120,3 +121,109 @@ def test_geometry_against_compiled_reference_random_cases(po):
         b = gc.run(inp, po, ref=False)
         for k in a:
             assert np.array_equal(a[k], b[k]), (seed, k)
+
+
+def test_geometry_random_axes_against_compiled_reference(po):
+    """Random axes, positions and sizes (not only random data): windows,
+    source points, receiver cells, random boundaries, FD step and compute
+    sizes of the oracle against the reference's own code."""
+    if po.ref_geom_lib() is None:
+        pytest.skip("reference sources not present")
+    R, L = po.ref_geom_lib(), po.port_lib()
+    f, i = po.fptr, po.iptr
+    f32 = np.float32
+    rng = np.random.default_rng(2024)
+    # image windows
+    for _ in range(25):
+        wn = tuple(int(x) for x in rng.integers(5, 15, 3))
+        wo = tuple(float(f32(x)) for x in rng.uniform(-50, 50, 3))
+        wd = tuple(float(f32(x)) for x in rng.uniform(3, 15, 3))
+        sn = tuple(int(x) for x in rng.integers(3, 17, 3))
+        so = tuple(float(f32(f32(o) + f32(k) * f32(d)))
+                   for o, k, d in zip(wo, rng.uniform(-8, 8, 3), wd))
+        whole = rng.standard_normal(wn[::-1]).astype(np.float32)
+        sub = rng.standard_normal(sn[::-1]).astype(np.float32)
+        off = [L.oracle_window_offset(so[a], wo[a], wd[a]) for a in range(3)]
+        a, b = np.zeros(sn[::-1], np.float32), np.zeros(sn[::-1], np.float32)
+        R.ref_geom_image_window(1, f(whole.copy()), *wn, *wo, *wd, f(a), *sn,
+                                *so, *wd)
+        L.oracle_extract_sub(f(whole), *wn, f(b), *sn, *off)
+        assert np.array_equal(a, b), (wn, wo, wd, sn, so)
+        wa, wb = whole.copy(), whole.copy()
+        R.ref_geom_image_window(0, f(wa), *wn, *wo, *wd, f(sub.copy()), *sn,
+                                *so, *wd)
+        L.oracle_add_image(f(wb), *wn, f(sub), *sn, *off)
+        assert np.array_equal(wa, wb), (wn, wo, wd, sn, so)
+    # source points and wavelet derivative on random grids
+    raw = rng.standard_normal(64).astype(np.float32)
+    for _ in range(12):
+        n = tuple(int(x) for x in rng.integers(24, 48, 3))
+        o = tuple(float(f32(x)) for x in rng.uniform(-200, 0, 3))
+        d = tuple(float(f32(x)) for x in rng.uniform(5, 12, 3))
+        pos = [float(f32(o[k] + rng.uniform(3, n[k] - 3) * d[k]))
+               for k in range(3)]
+        dt = float(f32(rng.uniform(5e-4, 2e-3)))
+        nts = 70
+        wd_ = np.zeros_like(raw)
+        L.oracle_wavelet_deriv(f(raw), raw.size, dt, f(wd_))
+        lr, lo = np.zeros(9, np.int32), np.zeros(9, np.int32)
+        vr = np.zeros(9 * nts, np.float32)
+        vo = np.zeros(9 * nts, np.float32)
+        R.ref_geom_source(f(raw), raw.size, dt, *pos, *o, *d, *n, nts, i(lr),
+                          f(vr))
+        L.oracle_source_geometry(*pos, *o, *d, n[0], n[1], f(wd_), raw.size,
+                                 nts, i(lo), f(vo))
+        assert np.array_equal(lr, lo) and np.array_equal(vr, vo), (n, o, d)
+    # receiver cells
+    for _ in range(12):
+        n = tuple(int(x) for x in rng.integers(40, 64, 3))
+        o = tuple(float(f32(x)) for x in rng.uniform(-100, 0, 3))
+        d = tuple(float(f32(x)) for x in rng.uniform(5, 12, 3))
+        rnx, rny = (int(x) for x in rng.integers(2, 12, 2))
+        rx0, ry0 = (float(f32(o[k] + rng.uniform(1, 5) * d[k]))
+                    for k in range(2))
+        rdx, rdy = (float(f32(x)) for x in rng.uniform(1, 3, 2) * d[0])
+        rz = float(f32(o[2] + rng.uniform(2, 10) * d[2]))
+        lr = np.zeros(rnx * rny, np.int32)
+        lo = np.zeros_like(lr)
+        R.ref_geom_receivers(rnx, rny, rx0, rdx, ry0, rdy, rz, *o, *d, *n, 40,
+                             i(lr))
+        L.oracle_receiver_geometry(rnx, rny, rx0, rdx, ry0, rdy, rz, *o, *d,
+                                   n[0], n[1], i(lo))
+        assert np.array_equal(lr, lo), (n, o, d, rnx, rny)
+    # random boundary on random compute grids
+    vel = (1500 + 2500 * rng.random((20, 22, 24))).astype(np.float32)
+    for _ in range(6):
+        n = tuple(int(x) for x in rng.integers(24, 36, 3))
+        o = tuple(float(f32(x)) for x in rng.uniform(-80, 0, 3))
+        d = (10.0, 10.0, 10.0)
+        nr = int(rng.integers(0, 9))
+        irand = int(rng.integers(0, 10000))
+        a = np.zeros(n[::-1], np.float32)
+        b = np.zeros_like(a)
+        va = (24, 22, 20, 0.0, 0.0, 0.0, 10.0, 10.0, 10.0)
+        R.ref_geom_rand_subspace(f(vel), *va, irand, nr, nr, nr, 0.001, *n,
+                                 *o, *d, f(a))
+        L.oracle_rand_subspace(f(vel), *va, float(vel.max()), irand, nr, nr,
+                               nr, 0.001, *n, *o, *d, f(b))
+        assert np.array_equal(a, b), (n, o, nr, irand)
+    # FD step and compute sizes
+    for _ in range(20):
+        vmax = float(f32(rng.uniform(1500, 6000)))
+        dv = float(f32(rng.uniform(2, 20)))
+        dtd = float(f32(rng.choice([5e-4, 1e-3, 2e-3, 4e-3])))
+        ntd = int(rng.integers(100, 3000))
+        v = np.full((6, 5, 4), 1500.0, np.float32)
+        v[2, 2, 2] = vmax
+        dt_r, nt_r = np.zeros(1, np.float32), np.zeros(1, np.int32)
+        R.ref_geom_calc_stability(f(v), 4, 5, 6, dv, dv, dv, dtd, ntd,
+                                  f(dt_r), i(nt_r))
+        nt_o = C.c_int()
+        dt_o = L.oracle_calc_stability(vmax, dv, dtd, ntd, C.byref(nt_o))
+        assert np.float32(dt_o) == dt_r[0] and nt_o.value == nt_r[0], (
+            vmax, dv, dtd, ntd)
+        nm, nb, fat = (int(x) for x in (rng.integers(9, 700),
+                                        rng.integers(0, 80),
+                                        rng.integers(0, 6)))
+        assert R.ref_geom_compute_size(nm, nb, fat) == \
+            L.oracle_compute_size(nm, nb, fat)
