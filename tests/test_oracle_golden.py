@@ -73,6 +73,24 @@ def test_port_against_compiled_reference_random_cases(po):
             assert np.array_equal(a[k], b[k]), (seed, k)
 
 
+def test_port_against_compiled_reference_random_shapes(po):
+    """Random grid shapes (odd sizes included), sinc ratios jt 1-4 and step
+    counts, with and without duplicated receivers."""
+    if po.ref_lib() is None:
+        pytest.skip("reference sources not present")
+    rng = np.random.default_rng(77)
+    for k in range(6):
+        shape = tuple(int(x) for x in rng.integers(14, 27, 3))
+        jt = int(rng.integers(1, 5))
+        nt = int(rng.integers(2, 30))
+        c = cases.make_case(100 + k, shape=shape, nt=nt, jt=jt,
+                            dup_receivers=int(k % 2), sinc=po.sinc_table)
+        a = po.run_case(po.RefProp(), c)
+        b = po.run_case(po.PortProp(), c)
+        for key in a:
+            assert np.array_equal(a[key], b[key]), (shape, jt, nt, key)
+
+
 def test_primitives_against_compiled_reference(po):
     if po.ref_lib() is None:
         pytest.skip("reference sources not present")
