@@ -202,3 +202,18 @@ def test_stream_mix_ceiling_measures(gpu):
     for r, w in ((1, 1), (7, 3)):
         gbs = gpu.stream_mix_gbs(r, w, n, reps=3)
         assert 500.0 < gbs < 20000.0, (r, w, gbs)
+
+
+def test_gpu_matches_oracle_random_shapes(gpu, po):
+    """Random grid shapes (nx a multiple of 4, the other axes any size >= 9
+    plus the stencil halo), sinc ratios and step counts, default tiling."""
+    rng = np.random.default_rng(91)
+    for k in range(4):
+        shape = (int(rng.integers(14, 40)), int(rng.integers(14, 40)),
+                 4 * int(rng.integers(5, 12)))
+        jt = int(rng.integers(1, 4))
+        nt = int(rng.integers(3, 25))
+        c = cases.make_case(200 + k, shape=shape, nt=nt, jt=jt,
+                            dup_receivers=int(k % 2), sinc=po.sinc_table)
+        got = po.run_case(gpu.Gb300Prop(), c)
+        check(got, po.run_case(po.PortProp(), c))
