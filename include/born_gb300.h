@@ -320,6 +320,13 @@ int born_tuned_config(const born_handle *h, int mode, int *cfg,
  * the last refinement of the mode measured for tile configuration c (0 when
  * not measured), for c < n, under the current storage. */
 int born_loop_tile_ms(const born_handle *h, int mode, float *ms, int n);
+/* Failure-detection self-test: launches one kernel whose bounded device
+ * wait (the step kernels' wait on their TMA copies) waits on something that
+ * never completes; after about 2 s it gives up, sets the handle's error word
+ * and returns.  Returns BORN_ETIMEOUT when detection works; the error word is
+ * then cleared and the handle stays usable.  No reference counterpart (the
+ * reference's kernels do not wait on each other). */
+int born_selftest_wait_timeout(born_handle *h);
 /* Kernels launched on this handle since creation (for accounting). */
 long long born_kernel_launches(const born_handle *h);
 

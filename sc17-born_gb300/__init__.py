@@ -92,6 +92,7 @@ _SIGS = {
     "born_autotune": (C.c_int, [_vp, C.c_int]),
     "born_tuned_config": (C.c_int, [_vp, C.c_int, _ip, _fp]),
     "born_loop_tile_ms": (C.c_int, [_vp, C.c_int, _fp, C.c_int]),
+    "born_selftest_wait_timeout": (C.c_int, [_vp]),
     "born_stream_mix_gbs": (C.c_int, [C.c_int, C.c_int, C.c_longlong,
                                       C.c_int, _fp]),
     "born_kernel_launches": (C.c_longlong, [_vp]),

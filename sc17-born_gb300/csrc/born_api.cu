@@ -1291,6 +1291,17 @@ int born_synchronize(born_handle *h) {
   return check_device_error(h);
 }
 
+int born_selftest_wait_timeout(born_handle *h) {
+  if (!h) return BORN_EINVAL;
+  int rc = set_device(h);
+  if (rc) return rc;
+  rc = check_device_error(h);  // start from a clear error word
+  if (rc) return rc;
+  CK(h, born::launch_wait_timeout_probe(h->err_dev, h->stream));
+  h->launches++;
+  return check_device_error(h);  // BORN_ETIMEOUT, and the word is cleared
+}
+
 int born_tile_config_count(void) { return born::tile_cfg_count(); }
 
 int born_autotune(born_handle *h, int enable) {

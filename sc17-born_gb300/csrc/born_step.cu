@@ -32,6 +32,18 @@ __global__ void point_inject_kernel(const PointSet ps, int npts, void *field,
   }
 }
 
+// Failure-detection self-test: one thread waits, with the step kernels'
+// bounded wait, on an mbarrier that no copy or thread ever completes; when
+// the bound runs out it sets the error word and returns, as a step kernel
+// whose TMA copy was lost would.
+__global__ void wait_timeout_probe(unsigned int *err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  mbar_fence_init();
+  if (!mbar_wait_bounded(&bar, 0)) atomicOr(err, kErrWaitTimeout);
+}
+
 __global__ void divide_kernel(const float *a, const float *v, float *out,
                               long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -180,6 +192,11 @@ cudaError_t launch_level_reset(unsigned long long *lv, int buf,
 cudaError_t launch_level_copy(unsigned long long *lv, int dst, int src,
                               unsigned int tag, cudaStream_t stream) {
   level_copy_kernel<<<1, 32, 0, stream>>>(lv, dst, src, tag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wait_timeout_probe(unsigned int *err, cudaStream_t stream) {
+  wait_timeout_probe<<<1, 32, 0, stream>>>(err);
   return cudaGetLastError();
 }
 

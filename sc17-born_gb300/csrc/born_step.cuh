@@ -227,5 +227,8 @@ cudaError_t launch_absmax(const float *x, long long n, unsigned int *out,
 // out[i] = a[i] / v[i] over the whole grid (image of the exact adjoint).
 cudaError_t launch_divide(const float *a, const float *v, float *out,
                           long long n, cudaStream_t stream);
+// One bounded wait that runs out (about 2 s) and sets kErrWaitTimeout in
+// *err: the failure-detection self-test.
+cudaError_t launch_wait_timeout_probe(unsigned int *err, cudaStream_t stream);
 
 }  // namespace born

@@ -217,3 +217,16 @@ def test_gpu_matches_oracle_random_shapes(gpu, po):
                             dup_receivers=int(k % 2), sinc=po.sinc_table)
         got = po.run_case(gpu.Gb300Prop(), c)
         check(got, po.run_case(po.PortProp(), c))
+
+
+def test_bounded_wait_gives_up_with_status_and_handle_stays_usable(gpu, po):
+    """Failure detection without a GPU fault: a bounded wait on an mbarrier
+    that nothing completes gives up (about 2 s), the host reads
+    BORN_ETIMEOUT, and the same handle then propagates bit-exactly."""
+    prop = gpu.Gb300Prop()
+    c = cases.make_case(51, shape=(20, 24, 28), nt=12, jt=1,
+                        sinc=po.sinc_table)
+    po.run_case(prop, c, which="none")  # grid and inputs in place
+    assert prop.lib.born_selftest_wait_timeout(prop.h) == -5
+    assert prop.lib.born_synchronize(prop.h) == 0  # error word cleared
+    check(po.run_case(prop, c), po.run_case(po.PortProp(), c))
