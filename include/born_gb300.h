@@ -308,7 +308,10 @@ int born_set_tiling(born_handle *h, int tile_cfg, int zseg);
 /* Autotuner: with enable != 0, times every tile configuration of each step
  * mode on the current grid now (needs the grid and both velocities) and
  * uses the fastest; time loops also tune a mode lazily on first use while
- * enabled and no fixed tiling is set.  enable = 0 turns it off. */
+ * enabled and no fixed tiling is set, and a loop of 400 steps or more then
+ * refines the choice on its own steps (every tile gives the same results;
+ * born_loop_tile_ms reports what it measured).  enable = 0 turns both off.
+ * A new grid (born_create_space) clears every choice. */
 int born_autotune(born_handle *h, int enable);
 /* Tile configuration in use for a step mode (0 source, 1 rtm forward,
  * 2 rtm adjoint, 3 modelling, 4 linearised forward, 5 its adjoint) and the
