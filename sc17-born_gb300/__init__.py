@@ -74,6 +74,9 @@ _SIGS = {
     "born_get_velocity": (C.c_int, [_vp, C.c_int, _fp]),
     "born_source_prop": (C.c_int, [_vp, C.c_int, C.c_int, _fp, _fp]),
     "born_rtm_adjoint": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _fp]),
+    "born_set_host_levels": (C.c_int, [_vp, C.c_int]),
+    "born_rtm_adjoint_host": (C.c_int, [_vp, C.c_int, C.c_int, _fp, _fp,
+                                        _fp]),
     "born_rtm_forward": (C.c_int, [_vp, C.c_int, C.c_int, _fp]),
     "born_model": (C.c_int, [_vp, C.c_int, C.c_int, _fp]),
     "born_lin_forward": (C.c_int, [_vp, C.c_int, C.c_int, _fp]),
@@ -343,24 +346,31 @@ class Gb300Prop(Handle):
                                                    fptr(rec)))
 
     def sourceProp(self, nx, ny, nz, damp, getLast, p0, p1, jts, npts, nt):
-        out0 = fptr(p0) if getLast and p0 is not None else None
-        out1 = fptr(p1) if getLast and p1 is not None else None
+        """The final levels are written into p0/p1 whatever getLast says, as
+        cpuProp does (cpu_prop.cc:106-129), and kept on the device."""
+        out0 = fptr(p0) if p0 is not None else None
+        out1 = fptr(p1) if p1 is not None else None
         self.check(self.lib.born_source_prop(self.h, jts, nt, out0, out1))
         self._src_arrays = (p0, p1)
 
+    HOST_LEVELS = {"resident": 0, "verify": 1, "upload": 2}
+
+    def set_host_levels(self, policy: str = "resident"):
+        """How rtmAdjoint reads its source-level arrays: "resident" (the
+        arrays sourceProp filled select the device-resident levels, their
+        contents unread), "verify" (the same, unless a checksum shows the
+        arrays changed since sourceProp wrote them) or "upload" (always
+        read, as cpuProp does)."""
+        self.check(self.lib.born_set_host_levels(self.h,
+                                                 self.HOST_LEVELS[policy]))
+
     def rtmAdjoint(self, n1, n2, n3, jtd, p0, p1, img, npts_s, nt):
-        a0, a1 = self._src_arrays
-        if p0 is a1 and p1 is a0:
-            swap = 1
-        elif p0 is a0 and p1 is a1:
-            swap = 0
-        else:  # levels supplied by the caller
-            self.check(self.lib.born_set_source_levels(self.h, fptr(f32(p0)),
-                                                       fptr(f32(p1))))
-            self._src_arrays = (p0, p1)
-            swap = 0
-        self.check(self.lib.born_rtm_adjoint(self.h, jtd, nt, swap,
-                                             fptr(img)))
+        # the arrays must keep their addresses for the pointer comparison
+        assert p0.dtype == np.float32 and p0.flags.c_contiguous
+        assert p1.dtype == np.float32 and p1.flags.c_contiguous
+        self.check(self.lib.born_rtm_adjoint_host(self.h, jtd, nt, fptr(p0),
+                                                  fptr(p1), fptr(img)))
+        self._src_arrays = (p0, p1)
 
     def rtmForward(self, n1, n2, n3, jt, img, rec, npts, nt, nt_big, rec_nx,
                    rec_ny):
@@ -617,31 +627,51 @@ class BornOperator(Handle):
         assert tuple(t.shape) == tuple(shape), (t.shape, shape)
         return C.c_void_p(t.data_ptr())
 
+    def _ordered(self, fn):
+        """Runs fn (which queues work on the handle's own stream) between
+        two cross-stream waits: the handle's stream first waits for what
+        torch's current stream has queued (the tensors passed in may still
+        be being written there), and torch's current stream then waits for
+        the handle's work (so a tensor written here is complete for whatever
+        torch runs next).  Neither side blocks the host."""
+        import torch
+        cur = torch.cuda.current_stream(self.device)
+        own = torch.cuda.ExternalStream(self.stream, device=self.device)
+        own.wait_stream(cur)
+        try:
+            return fn()
+        finally:
+            cur.wait_stream(own)
+
     def forward(self, add, model, data):
-        self.check(self.lib.born_op_forward(
-            self.op, int(add), self._dev(model, self.model_shape),
-            self._dev(data, self.data_shape)))
+        m = self._dev(model, self.model_shape)
+        d = self._dev(data, self.data_shape)
+        self._ordered(lambda: self.check(self.lib.born_op_forward(
+            self.op, int(add), m, d)))
         return True
 
     def adjoint(self, add, model, data):
-        self.check(self.lib.born_op_adjoint(
-            self.op, int(add), self._dev(model, self.model_shape),
-            self._dev(data, self.data_shape)))
+        m = self._dev(model, self.model_shape)
+        d = self._dev(data, self.data_shape)
+        self._ordered(lambda: self.check(self.lib.born_op_adjoint(
+            self.op, int(add), m, d)))
         return True
 
     def dot(self, a, b):
+        assert a.is_cuda and b.is_cuda and a.numel() == b.numel()
         out = C.c_double()
-        self.check(self.lib.born_dot_f64(self.op, C.c_void_p(a.data_ptr()),
-                                         C.c_void_p(b.data_ptr()), a.numel(),
-                                         C.byref(out)))
+        self._ordered(lambda: self.check(self.lib.born_dot_f64(
+            self.op, C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
+            a.numel(), C.byref(out))))
         return out.value
 
     def cg(self, data, model, niter):
         """Least squares by cgstep CG; model is updated in place."""
         res = (C.c_double * (niter + 1))()
-        self.check(self.lib.born_cg_solve(
-            self.op, self._dev(data, self.data_shape),
-            self._dev(model, self.model_shape), niter, res))
+        d = self._dev(data, self.data_shape)
+        m = self._dev(model, self.model_shape)
+        self._ordered(lambda: self.check(self.lib.born_cg_solve(
+            self.op, d, m, niter, res)))
         return list(res)
 
 
@@ -692,6 +722,29 @@ def receiver_geometry(rec_nx, rec_ny, rx0, rdx, ry0, rdy, rz, o, d, n1, n2):
                                      o[0], o[1], o[2], d[0], d[1], d[2], n1,
                                      n2, iptr(locs)))
     return locs
+
+
+def extract_sub(whole, shape, offsets):
+    """Window of ``shape`` (n3, n2, n1) cut from the model-grid array
+    ``whole`` starting at sample ``offsets`` (f1, f2, f3) of its axes 1..3
+    (image_rtm_3d.cc:53-95); cells outside ``whole`` are zero."""
+    whole = f32(whole)
+    w3, w2, w1 = whole.shape
+    s3, s2, s1 = shape
+    out = np.zeros(shape, np.float32)
+    _ck(lib().born_extract_sub(fptr(whole), w1, w2, w3, fptr(out), s1, s2, s3,
+                               offsets[0], offsets[1], offsets[2]))
+    return out
+
+
+def laplac_forward(m):
+    """The reference's laplac forward, a first difference along z
+    (laplac_3d.cc:51-105)."""
+    m = f32(m)
+    n3, n2, n1 = m.shape
+    out = np.zeros_like(m)
+    _ck(lib().born_laplac_forward(0, fptr(m), fptr(out), n1, n2, n3))
+    return out
 
 
 def rand_subspace(vel, vo, vd, vmax, irand, nrand, dt, shape, o, d):

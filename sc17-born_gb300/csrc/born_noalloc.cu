@@ -22,7 +22,14 @@
 //
 // The array's address is looked up once per device (cudaGetSymbolAddress,
 // with that device current) on the first call made on the device; make that
-// first call before any stream capture begins.
+// first call before any stream capture begins.  The looked-up address is
+// kept for the life of the process (device indices below kMaxDevices); a
+// cudaDeviceReset reloads the module and leaves it stale, so the function
+// must not be called again on a device that was reset.
+//
+// A CUDA error that the calling thread already has pending is not ours to
+// clear: the call then returns BORN_ECUDA without launching, and the caller
+// still finds its own error with cudaGetLastError.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -111,6 +118,9 @@ int born_dot_f64_noalloc(const float *a, const float *b, long long n,
                  n, (long long)BORN_DOT_NOALLOC_MAX, kNoAllocPartials);
     return BORN_EINVAL;
   }
+  // an earlier failure of the caller's stays pending and is not reported
+  // as ours by the launch checks below
+  if (cudaPeekAtLastError() != cudaSuccess) return BORN_ECUDA;
   double *scratch = nullptr;
   int rc = scratch_for_current_device(&scratch);
   if (rc) return rc;

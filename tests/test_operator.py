@@ -258,3 +258,43 @@ def test_cg_matches_fp64_restatement(born, torch_cuda):
         rr += ss
     assert rel(m_gpu.cpu().numpy(), m) <= 1e-3
     assert abs(res[-1] - np.vdot(rr, rr)) <= 1e-3 * res[-1]
+
+
+def test_operator_orders_after_torch_stream(born, torch_cuda):
+    """The operator's work runs on the handle's own stream; tensors that
+    torch is still producing on its current stream must be complete before
+    the operator reads them, and the operator's output must be complete for
+    the torch work queued after it.  The input here is written behind a
+    long device sleep on torch's stream, and the output is cloned on that
+    stream right after the call."""
+    torch = torch_cuda
+    kw = setup_problem(seed=6, nshots=1, nt_data=40)
+    op = born.BornOperator(exact=True, ckpt_interval=10, **kw)
+    g = torch.Generator(device="cuda").manual_seed(77)
+    m_src = torch.randn(op.model_shape, device="cuda", generator=g)
+    d_src = torch.randn(op.data_shape, device="cuda", generator=g)
+    want_d = torch.zeros(op.data_shape, device="cuda")
+    want_m = torch.zeros(op.model_shape, device="cuda")
+    op.forward(False, m_src, want_d)
+    op.adjoint(False, want_m, d_src)
+    want_dot = op.dot(m_src, want_m)
+    torch.cuda.synchronize()
+    for _ in range(2):
+        m = torch.zeros(op.model_shape, device="cuda")
+        d = torch.zeros(op.data_shape, device="cuda")
+        torch.cuda._sleep(200_000_000)  # ~0.1 s of device time
+        m.copy_(m_src)                  # still queued when forward starts
+        d.copy_(d_src)
+        out_d = torch.zeros(op.data_shape, device="cuda")
+        op.forward(False, m, out_d)
+        got_d = out_d.clone()           # torch's stream, right after
+        torch.cuda._sleep(200_000_000)
+        m2 = m_src * 1.0
+        got_dot = op.dot(m2, want_m)
+        out_m = torch.zeros(op.model_shape, device="cuda")
+        op.adjoint(False, out_m, d)
+        got_m = out_m.clone()
+        torch.cuda.synchronize()
+        assert torch.equal(got_d, want_d)
+        assert torch.equal(got_m, want_m)
+        assert got_dot == want_dot
