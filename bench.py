@@ -195,8 +195,7 @@ def aggregate_rate(cells_per_rank: float, steps: int, t_ms_max: float,
 def cpu_sample(case, threads: int, kind: str, budget_s: float = 20.0):
     """Gcell-updates/s of the CPU implementation on a truncated-nt sample of
     the same grid: Born forward + source propagation + RTM adjoint."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle as po
+    po = oracle_module()
     if kind == "reference" and po.ref_lib() is not None:
         os.environ["ORACLE_REF_THREADS"] = str(threads)
         mk = po.RefProp
@@ -215,11 +214,13 @@ def cpu_sample(case, threads: int, kind: str, budget_s: float = 20.0):
 
     probe_nt = 2
     t = run(probe_nt)
-    per_step = t / probe_nt
-    nt = int(max(2, min(200, budget_s / max(per_step, 1e-9))))
-    t = run(nt)
+    nt = probe_nt
+    if budget_s > 0:
+        per_step = t / probe_nt
+        nt = int(max(2, min(200, budget_s / max(per_step, 1e-9))))
+        t = run(nt)
     rate = 2.0 * n_int * nt / t / 1e9
-    return {"value": round(rate, 4), "unit": "Gcell-updates/s",
+    return {"value": round(rate, 4), "unit": "Gcell-updates/s", "nt": nt,
             "cores": threads, "kind": "reference" if kind == "reference" else "port",
             "sample": f"{case['name']} grid {case['shape'][2]}x{case['shape'][1]}x"
                       f"{case['shape'][0]}, Born forward + source propagation + "
@@ -227,37 +228,72 @@ def cpu_sample(case, threads: int, kind: str, budget_s: float = 20.0):
                       f"({t:.1f} s)"}
 
 
+def arm_config(case, storage: str, world: int) -> dict:
+    """The ``config`` object of the c1/c2 line, printed identically by the
+    GPU arm and the reference arm."""
+    nz, ny, nx = case["shape"]
+    n_int = (nx - 8) * (ny - 8) * (nz - 8)
+    return {"workload": f"{case['name']}: 3D Born forward + RTM adjoint, "
+            f"compute grid {nx}x{ny}x{nz}, nt={case['nt']}, "
+            "random-boundary source reconstruction",
+            "grid": [nz, ny, nx], "nt": case["nt"], "jt": case["jts"],
+            "interior_cells": n_int, "storage": storage,
+            "l2": "inputs larger than L2 (7 x %.0f MB fields)" %
+                  (nx * ny * nz * 4 / 1e6),
+            "parallelism": f"shots x{world} (one per GPU)" +
+            (", image summed over the ranks every step (NCCL all-reduce)"
+             if world > 1 else "")}
+
+
+def oracle_module():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    return pyoracle
+
+
 def run_reference_arm(args):
+    """The reference's CPU path on the host cores: the compiled reference
+    cpuProp where it exists on this machine, else the C restatement (the
+    oracle port).  The shot's inputs come from the restatement's own
+    geometry (pinned bit for bit to the reference's sources), so this arm
+    loads no library of the product.  A full c2 step (nt = 2000) takes
+    minutes on the CPU, so each timed step is a truncated-nt sample of the
+    same shot and ms_per_step is extrapolated from it."""
     rank, world, local = dist_env()
     if rank != 0:
         return 0
-    born = package()
-    born.build()
+    po = oracle_module()
     wl = workload_module()
-    case = wl.prepare_shot(born, args.config, nt=args.nt, n=args.model_n)
+    case = wl.prepare_shot(po.Geometry(), args.config, nt=args.nt,
+                           n=args.model_n)
     threads = os.cpu_count() or 1
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle as po
     kind = "reference" if po.ref_lib() is not None else "port"
-    vals = []
-    for i in range(args.warmup + args.steps):
-        r = cpu_sample(case, threads, kind, budget_s=args.cpu_budget /
-                       max(1, args.steps))
-        if i >= args.warmup:
-            vals.append(r["value"])
+    # each timed sample gets an equal share of the CPU budget (at least a
+    # few seconds); the warm-up samples are two-step runs
+    per_sample = max(3.0, args.ref_budget / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_sample(case, threads, kind, budget_s=0.0)
+    vals, last = [], None
+    for _ in range(args.steps):
+        last = cpu_sample(case, threads, kind, budget_s=per_sample)
+        vals.append(last["value"])
     v = statistics.median(vals)
     n_int = wl.interior_cells(case["shape"])
     line = {
         "metric": "Gcell-updates/s Born fwd+adj", "value": v,
         "unit": "Gcell-updates/s", "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 2.0 * n_int * case["nt"] / (v * 1e9) * 1e3,
+        "ms_per_step": round(2.0 * n_int * case["nt"] / (v * 1e9) * 1e3, 1),
+        "ms_per_step_extrapolated": True,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded, shapes of the config)",
-        "config": {"workload": f"{args.config}: 3D Born forward + RTM adjoint, "
-                   f"compute grid {case['shape'][2]}^3, nt={case['nt']}",
-                   "grid": list(case["shape"]), "nt": case["nt"]},
-        "cpu_baseline": dict(r, value=v),
+        "config": arm_config(case, "f32", world),
+        "sample_nt": last["nt"],
+        "note": "each timed step is a sample of nt=%d of the %d FD steps of "
+                "the shot (Born forward + source propagation + RTM adjoint);"
+                " ms_per_step is extrapolated linearly to the full nt" %
+                (last["nt"], case["nt"]),
+        "cpu_baseline": dict(last, value=v),
         "e2e": {"value": v, "unit": "Gcell-updates/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -415,17 +451,7 @@ def run_gpu_arm(args):
             "dtype": "f32" if (args.storage or "f32") == "f32" else
                      "f32 arithmetic; levels " + args.storage,
             "data": "synthetic (seeded, shapes of the config)",
-            "config": {"workload": f"{args.config}: 3D Born forward + RTM "
-                       f"adjoint, compute grid {nx}x{ny}x{nz}, nt={nt}, "
-                       "random-boundary source reconstruction",
-                       "grid": [nz, ny, nx], "nt": nt, "jt": jt,
-                       "interior_cells": n_int,
-                       "storage": args.storage or "f32",
-                       "l2": "inputs larger than L2 (7 x %.0f MB fields)" %
-                             (nx * ny * nz * 4 / 1e6),
-                       "parallelism": f"shots x{world} (one per GPU)" +
-                       (", image summed over the ranks every step (NCCL "
-                        "all-reduce)" if world > 1 else "")},
+            "config": arm_config(case, args.storage or "f32", world),
             # one shot-step: a time step of one shot's Born forward + RTM
             # adjoint (source propagation included), over all ranks
             "shot_steps_per_s": round(world * nt * args.steps / (t_ms / 1e3),
@@ -788,7 +814,11 @@ def main():
     ap.add_argument("--tile", type=int, default=-1)
     ap.add_argument("--zseg", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--cpu-budget", type=float, default=20.0,
+                    help="seconds of CPU work for the cpu_baseline sample")
+    ap.add_argument("--ref-budget", type=float, default=100.0,
+                    help="--impl reference: seconds of CPU work over all "
+                         "timed samples")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fused", action="store_true",

@@ -84,10 +84,11 @@ void source_prop(int n1, int n2, int n3, bool damp, bool get_last, float *p0,
 
 /* gpu_funcs_3d.h:13-14 (rtm_adjoint, gpu_funcs_3d.cu:832-1154).  Reverse-time
  * RTM adjoint (cpu_prop.cc:56-96).  p0_s_cpu/p1_s_cpu name the two source
- * levels: when they are the host arrays last given to source_prop (in either
- * order) the device-resident levels are used in that order; other non-null
- * arrays are uploaded.  The full padded image is accumulated onto img (zero
- * on entry at every reference call site, rtm_zero_op_3d.cc:259). */
+ * levels, read as born_rtm_adjoint_host reads them (by default: when they are
+ * the host arrays last given to source_prop, in either order, the
+ * device-resident levels are used in that order; other non-null arrays are
+ * uploaded).  The full padded image is accumulated onto img (zero on entry at
+ * every reference call site, rtm_zero_op_3d.cc:259). */
 void rtm_adjoint(int n1, int n2, int n3, int j, float *p0_s_cpu,
                  float *p1_s_cpu, float *img, int npts, int nt);
 
@@ -157,6 +158,31 @@ int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
  * contents, as cpuProp does (cpu_prop.cc:101); null starts from zero and
  * leaves the image on the device. */
 int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap, float *img);
+
+/* baseProp::rtmAdjoint(..., p0, p1, img, ...) (base_prop.h:57-62) on host
+ * arrays of the two source levels, as the reference's operator calls it
+ * after sourceProp (rtm_zero_op_3d.cc:272-282).  How p0/p1 are read is the
+ * handle's host-level policy (born_set_host_levels):
+ *  BORN_HOST_LEVELS_RESIDENT (default): like the reference's GPU path, which
+ *    keeps the source levels on the device (gpu_funcs_3d.cu:14,436-445):
+ *    when p0/p1 are the arrays the last born_source_prop wrote (in either
+ *    order) the device-resident levels are used in that order, and their
+ *    contents are not read; any other arrays are uploaded;
+ *  BORN_HOST_LEVELS_VERIFY: as RESIDENT, but born_source_prop records a
+ *    64-bit checksum of each host array it writes and this call re-computes
+ *    it: arrays whose contents changed since are uploaded;
+ *  BORN_HOST_LEVELS_UPLOAD: like cpuProp, the arrays are always read (one
+ *    upload of both levels per call).
+ * The device levels are advanced by the reverse-time reconstruction, as
+ * cpuProp advances the arrays it is given; a second call on unchanged
+ * arrays continues from there under RESIDENT and VERIFY.  p0/p1 non-null;
+ * FP32 level storage when an upload is needed. */
+#define BORN_HOST_LEVELS_RESIDENT 0
+#define BORN_HOST_LEVELS_VERIFY 1
+#define BORN_HOST_LEVELS_UPLOAD 2
+int born_set_host_levels(born_handle *h, int policy);
+int born_rtm_adjoint_host(born_handle *h, int jtd, int nt, const float *p0,
+                          const float *p1, float *img);
 int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out);
 
 /* Nonlinear modelling through vel2 with the taper (the background of
@@ -286,7 +312,12 @@ int born_batch_synchronize(born_batch *b);
  * limited to BORN_DOT_NOALLOC_MAX elements; larger n returns BORN_EINVAL.
  * All calls share that array: calls that overlap on the GPU race.  The first
  * call on a device looks up the array's address on that device; make it
- * before any stream capture begins. */
+ * before any stream capture begins.  The address is kept for the life of
+ * the process, for device indices 0..63 (higher indices return
+ * BORN_ENODEV); after cudaDeviceReset the kept address is stale, so do not
+ * call this function on a device that was reset.  If the calling thread
+ * already has a CUDA error pending, the call returns BORN_ECUDA and leaves
+ * that error pending (it launches nothing). */
 #define BORN_DOT_NOALLOC_MAX 268435456LL
 int born_dot_f64_noalloc(const float *a, const float *b, long long n,
                          double *out, void *stream);

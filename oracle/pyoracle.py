@@ -24,7 +24,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_cpuprop.so")
-REF_SRC = "/root/reference"
+# The reference checkout (its base/ folder holds cpu_prop.cc and the
+# geometry sources) comes from the environment; unset, only libraries built
+# earlier into _ref/ are used.
+REF_SRC = os.environ.get("SC17_BORN_REF") or None
 
 _fp = C.POINTER(C.c_float)
 _dp = C.POINTER(C.c_double)
@@ -41,7 +44,7 @@ def build_port(force: bool = False) -> str:
 
 def build_ref(force: bool = False) -> str | None:
     """Compile the reference CPU path when its sources are present here."""
-    if not os.path.isdir(os.path.join(REF_SRC, "base")):
+    if not REF_SRC or not os.path.isdir(os.path.join(REF_SRC, "base")):
         return REF_SO if os.path.exists(REF_SO) else None
     if force or not os.path.exists(REF_SO):
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"],
@@ -60,7 +63,7 @@ def ref_geom_lib():
     or None where the sources are absent."""
     global _ref_geom
     if _ref_geom is None:
-        if os.path.isdir(os.path.join(REF_SRC, "base")):
+        if REF_SRC and os.path.isdir(os.path.join(REF_SRC, "base")):
             subprocess.run(["make", "-s", "-C", HERE, "_ref/libref_geom.so",
                             f"REF={REF_SRC}"], check=True)
         if not os.path.exists(REF_GEOM_SO):
@@ -468,6 +471,90 @@ def sinc_table(ntab: int, nsinc: int = 8, ref: bool = False) -> np.ndarray:
     else:
         port_lib().oracle_sinc_table(ntab, nsinc, fptr(out))
     return out
+
+
+class Geometry:
+    """The host geometry and glue of the restatement (pinned bit for bit to
+    the reference's own sources) under the function names of the product's
+    host-geometry module, so that the shot builder can make a case's inputs
+    without the product library: calc_stability (fd_prop_3d.cc:6-33),
+    compute_size (source_func_3d.cc:4-61), sinc_table (sinc_bob.cc),
+    wavelet_deriv and source_geometry (source_func_3d.cc:76-127),
+    receiver_geometry (data_rtm_3d.cc:59-90, map_data_3d.cc:4-35),
+    rand_subspace (vel_fd_3d.cc:29-134), extract_sub (image_rtm_3d.cc:53-95)
+    and laplac_forward (laplac_3d.cc:51-105)."""
+
+    @staticmethod
+    def calc_stability(vmax, dmin, dt_data, nt_data):
+        nt = C.c_int(0)
+        dt = port_lib().oracle_calc_stability(vmax, dmin, dt_data, nt_data,
+                                              C.byref(nt))
+        return float(dt), int(nt.value)
+
+    @staticmethod
+    def compute_size(n_model, nbound, fat=4):
+        return int(port_lib().oracle_compute_size(n_model, nbound, fat))
+
+    @staticmethod
+    def sinc_table(ntab, nsinc=8):
+        return sinc_table(ntab, nsinc)
+
+    @staticmethod
+    def wavelet_deriv(raw, dt):
+        raw = _f32(raw)
+        out = np.zeros_like(raw)
+        port_lib().oracle_wavelet_deriv(fptr(raw), raw.size, dt, fptr(out))
+        return out
+
+    @staticmethod
+    def source_geometry(sx, sy, sz, o, d, n1, n2, wavelet, nts):
+        locs = np.zeros(9, np.int32)
+        vals = np.zeros((9, nts), np.float32)
+        w = _f32(wavelet)
+        port_lib().oracle_source_geometry(sx, sy, sz, o[0], o[1], o[2], d[0],
+                                          d[1], d[2], n1, n2, fptr(w), w.size,
+                                          nts, iptr(locs), fptr(vals))
+        return locs, vals
+
+    @staticmethod
+    def receiver_geometry(rec_nx, rec_ny, rx0, rdx, ry0, rdy, rz, o, d, n1,
+                          n2):
+        locs = np.zeros(rec_nx * rec_ny, np.int32)
+        port_lib().oracle_receiver_geometry(rec_nx, rec_ny, rx0, rdx, ry0, rdy,
+                                            rz, o[0], o[1], o[2], d[0], d[1],
+                                            d[2], n1, n2, iptr(locs))
+        return locs
+
+    @staticmethod
+    def rand_subspace(vel, vo, vd, vmax, irand, nrand, dt, shape, o, d):
+        vel = _f32(vel)
+        vn3, vn2, vn1 = vel.shape
+        n3, n2, n1 = shape
+        out = np.zeros(shape, np.float32)
+        port_lib().oracle_rand_subspace(
+            fptr(vel), vn1, vn2, vn3, vo[0], vo[1], vo[2], vd[0], vd[1], vd[2],
+            vmax, irand, nrand[0], nrand[1], nrand[2], dt, n1, n2, n3, o[0],
+            o[1], o[2], d[0], d[1], d[2], fptr(out))
+        return out
+
+    @staticmethod
+    def extract_sub(whole, shape, offsets):
+        whole = _f32(whole)
+        w3, w2, w1 = whole.shape
+        s3, s2, s1 = shape
+        out = np.zeros(shape, np.float32)
+        port_lib().oracle_extract_sub(fptr(whole), w1, w2, w3, fptr(out), s1,
+                                      s2, s3, offsets[0], offsets[1],
+                                      offsets[2])
+        return out
+
+    @staticmethod
+    def laplac_forward(m):
+        m = _f32(m)
+        n3, n2, n1 = m.shape
+        out = np.zeros_like(m)
+        port_lib().oracle_laplac_forward(0, fptr(m), fptr(out), n1, n2, n3)
+        return out
 
 
 # ---------------------------------------------------------------------------

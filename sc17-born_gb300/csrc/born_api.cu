@@ -670,6 +670,28 @@ void born_set_lp_words(born_handle *h, StepParams &p, int mode) {
   p.imgmax = st + kStatRefl;
 }
 
+// Checksum of a host level array for BORN_HOST_LEVELS_VERIFY: four
+// independent xor-multiply lanes over the 32-bit words (so the loop is not
+// one long dependency chain), folded at the end.  It detects any change a
+// caller makes to the array between source_prop and rtm_adjoint; it is not
+// meant to resist deliberate collisions.
+unsigned long long host_level_sum(const float *p, long long n) {
+  const unsigned int *w = reinterpret_cast<const unsigned int *>(p);
+  const unsigned long long K = 0x9E3779B97F4A7C15ull;
+  unsigned long long a = 1, b = 2, c = 3, d = 4;
+  long long i = 0;
+  for (; i + 4 <= n; i += 4) {
+    a = (a ^ w[i]) * K;
+    b = (b ^ w[i + 1]) * K;
+    c = (c ^ w[i + 2]) * K;
+    d = (d ^ w[i + 3]) * K;
+  }
+  for (; i < n; ++i) a = (a ^ w[i]) * K;
+  unsigned long long x = a ^ (b * 3) ^ (c * 5) ^ (d * 7) ^ (unsigned long long)n;
+  x ^= x >> 31;
+  return x * K;
+}
+
 // ===========================================================================
 // Handle API
 extern "C" {
@@ -880,9 +902,20 @@ int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
     if (rc) return rc;
   }
   h->src_levels_valid = true;
+  h->host_p0 = p0_out;
+  h->host_p1 = p1_out;
+  h->host_sums_valid = false;
   if (p0_out) CK(h, cudaMemcpyAsync(p0_out, h->s0, bytes, cudaMemcpyDeviceToHost, h->stream));
   if (p1_out) CK(h, cudaMemcpyAsync(p1_out, h->s1, bytes, cudaMemcpyDeviceToHost, h->stream));
-  if (p0_out || p1_out) return check_device_error(h);
+  if (p0_out || p1_out) {
+    rc = check_device_error(h);
+    if (rc) return rc;
+    if (h->host_levels == BORN_HOST_LEVELS_VERIFY && p0_out && p1_out) {
+      h->host_sum0 = host_level_sum(p0_out, h->n123);
+      h->host_sum1 = host_level_sum(p1_out, h->n123);
+      h->host_sums_valid = true;
+    }
+  }
   return BORN_OK;
 }
 
@@ -963,6 +996,56 @@ int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap,
     return check_device_error(h);
   }
   return BORN_OK;
+}
+
+int born_set_host_levels(born_handle *h, int policy) {
+  if (!h) return BORN_EINVAL;
+  if (policy != BORN_HOST_LEVELS_RESIDENT &&
+      policy != BORN_HOST_LEVELS_VERIFY && policy != BORN_HOST_LEVELS_UPLOAD)
+    return fail(h, BORN_EINVAL, "unknown host-level policy %d", policy);
+  h->host_levels = policy;
+  // checksums are only taken while verifying: a later source_prop makes them
+  h->host_sums_valid = false;
+  return BORN_OK;
+}
+
+// baseProp::rtmAdjoint on host arrays of the source levels (base_prop.h:57-62)
+int born_rtm_adjoint_host(born_handle *h, int jtd, int nt, const float *p0,
+                          const float *p1, float *img) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (!p0 || !p1) return fail(h, BORN_EINVAL, "null source level array");
+  int swap = -1;  // -1: upload p0/p1
+  if (h->host_levels != BORN_HOST_LEVELS_UPLOAD && h->src_levels_valid &&
+      h->host_p0 && h->host_p1) {
+    if (p0 == h->host_p1 && p1 == h->host_p0)
+      swap = 1;
+    else if (p0 == h->host_p0 && p1 == h->host_p1)
+      swap = 0;
+    if (swap >= 0 && h->host_levels == BORN_HOST_LEVELS_VERIFY) {
+      // the arrays still hold what source_prop wrote into them?
+      const bool same =
+          h->host_sums_valid &&
+          host_level_sum(h->host_p0, h->n123) == h->host_sum0 &&
+          host_level_sum(h->host_p1, h->n123) == h->host_sum1;
+      if (!same) swap = -1;
+    }
+  }
+  if (swap < 0) {
+    rc = born_set_source_levels(h, p0, p1);
+    if (rc) return rc;
+    // the device levels now mirror these arrays (s0 <- p0, s1 <- p1)
+    h->host_p0 = p0;
+    h->host_p1 = p1;
+    h->host_sums_valid = false;
+    if (h->host_levels == BORN_HOST_LEVELS_VERIFY) {
+      h->host_sum0 = host_level_sum(p0, h->n123);
+      h->host_sum1 = host_level_sum(p1, h->n123);
+      h->host_sums_valid = true;
+    }
+    swap = 0;
+  }
+  return born_rtm_adjoint(h, jtd, nt, swap, img);
 }
 
 // cpuProp::rtmForward, cpu_prop.cc:22-54
@@ -1471,7 +1554,9 @@ void source_prop(int n1, int n2, int n3, bool damp, bool get_last, float *p0,
     return record(fail(h, BORN_EINVAL, "source_prop: grid mismatch"));
   int rc = born_source_prop(h, jt, nt, get_last ? p0 : nullptr,
                             get_last ? p1 : nullptr);
-  if (rc == BORN_OK) {
+  if (rc == BORN_OK && !get_last) {
+    // the reference's GPU path keeps the levels on the device and ignores
+    // the host arrays (gpu_funcs_3d.cu:409-427): they still name them
     h->host_p0 = p0;
     h->host_p1 = p1;
   }
@@ -1485,19 +1570,9 @@ void rtm_adjoint(int n1, int n2, int n3, int j, float *p0_s_cpu,
   if (!h) return record(BORN_ENODEV);
   if (h->have_space && (n1 != h->n1 || n2 != h->n2 || n3 != h->n3))
     return record(fail(h, BORN_EINVAL, "rtm_adjoint: grid mismatch"));
-  int swap = 0;
-  const bool resident = h->src_levels_valid && p0_s_cpu && p1_s_cpu;
-  if (resident && p0_s_cpu == h->host_p1 && p1_s_cpu == h->host_p0) {
-    swap = 1;
-  } else if (resident && p0_s_cpu == h->host_p0 && p1_s_cpu == h->host_p1) {
-    swap = 0;
-  } else if (p0_s_cpu && p1_s_cpu) {
-    int rc = born_set_source_levels(h, p0_s_cpu, p1_s_cpu);
-    if (rc) return record(rc);
-    h->host_p0 = p0_s_cpu;
-    h->host_p1 = p1_s_cpu;
-  }
-  record(born_rtm_adjoint(h, j, nt, swap, img));
+  if (!p0_s_cpu || !p1_s_cpu)  // the device-resident levels as they are
+    return record(born_rtm_adjoint(h, j, nt, 0, img));
+  record(born_rtm_adjoint_host(h, j, nt, p0_s_cpu, p1_s_cpu, img));
 }
 
 void set_ntblock(int nt) {

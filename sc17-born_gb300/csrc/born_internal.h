@@ -72,7 +72,13 @@ struct born_handle {
   bool have_vel1 = false, have_vel2 = false, have_refl = false;
   DevPoints src, rec;
   bool src_levels_valid = false;
+  // host arrays the last source_prop wrote the levels to (s0 -> host_p0,
+  // s1 -> host_p1), the host-level policy of rtm_adjoint and, under
+  // BORN_HOST_LEVELS_VERIFY, checksums of the contents written
   const float *host_p0 = nullptr, *host_p1 = nullptr;
+  int host_levels = BORN_HOST_LEVELS_RESIDENT;
+  bool host_sums_valid = false;
+  unsigned long long host_sum0 = 0, host_sum1 = 0;
   int tile_cfg = -1, zseg = 0;
   // bumped whenever device buffers or point sets are reallocated, so that
   // cached descriptors and graphs built over them can notice

@@ -10,11 +10,15 @@
 //
 //  * transferReceiverFunc retains the trace array; rtmForward accumulates the
 //    modelled traces into it (cpu_prop.cc:205-212);
-//  * sourceProp leaves the final two levels in p0/p1 when getLast is set and
-//    keeps them on the device;
-//  * rtmAdjoint accepts the levels either as the arrays sourceProp filled
-//    (in either order, no copy) or as any other host arrays (uploaded), and
-//    accumulates the image into img (cpu_prop.cc:101).
+//  * sourceProp leaves the final two levels in p0/p1, as cpuProp does
+//    whatever getLast says (cpu_prop.cc:106-129), and keeps them on the
+//    device;
+//  * rtmAdjoint reads the levels through born_rtm_adjoint_host: by default
+//    the arrays sourceProp filled (in either order) select the
+//    device-resident levels without a copy and any other host arrays are
+//    uploaded; born_set_host_levels(handle(), ...) makes it verify the
+//    arrays' contents by checksum or always upload them.  The image is
+//    accumulated into img (cpu_prop.cc:101).
 //
 // Base is the class to derive from: in the reference tree,
 //   typedef gb300PropT<baseProp> gb300Prop;
@@ -95,26 +99,17 @@ class gb300PropT : public Base {
                           float *p0, float *p1, int jts, int npts, int nt) {
     (void)nx, (void)ny, (void)nz, (void)damp, (void)npts;
     if (!ready()) return;
-    if (done(born_source_prop(h_, jts, nt, getLast ? p0 : nullptr,
-                              getLast ? p1 : nullptr))) {
-      src0_ = p0;
-      src1_ = p1;
-    }
+    (void)getLast;
+    done(born_source_prop(h_, jts, nt, p0, p1));
   }
 
   virtual void rtmAdjoint(int n1, int n2, int n3, int jtd, float *p0,
                           float *p1, float *img, int npts_s, int nt) {
     (void)n1, (void)n2, (void)n3, (void)npts_s;
     if (!ready()) return;
-    int swap = 0;
-    if (p0 && p0 == src1_ && p1 == src0_) {
-      swap = 1;
-    } else if (!(p0 && p0 == src0_ && p1 == src1_)) {
-      if (!done(born_set_source_levels(h_, p0, p1))) return;
-      src0_ = p0;
-      src1_ = p1;
-    }
-    done(born_rtm_adjoint(h_, jtd, nt, swap, img));
+    // the handle's host-level policy decides whether p0/p1 are read or the
+    // device-resident levels source_prop left are used
+    done(born_rtm_adjoint_host(h_, jtd, nt, p0, p1, img));
   }
 
   virtual void rtmForward(int n1, int n2, int n3, int jt, float *img,
@@ -152,5 +147,4 @@ class gb300PropT : public Base {
   int status_ = BORN_OK;
   bool throw_ = false;
   float *rec_ = nullptr;
-  const float *src0_ = nullptr, *src1_ = nullptr;
 };

@@ -12,10 +12,15 @@ shapes, sizes and value ranges of the benchmark configurations:
 
 ``prepare_shot`` turns a model into the propagator inputs exactly as the
 reference's operator does per shot (rtm_zero_op_3d.cc:139-185 and
-:243-273), using this package's host geometry: compute grid and origin,
-sinc tables, 9-point source with the wavelet's time derivative, receiver
-cells, random-boundary and plain v^2 dt^2 models, and the reflectivity after
-the z first difference.
+:243-273): compute grid and origin, sinc tables, 9-point source with the
+wavelet's time derivative, receiver cells, random-boundary and plain v^2 dt^2
+models, and the reflectivity after the z first difference.  The geometry
+comes from ``geo``, any object with the host-geometry functions of this
+package (``calc_stability``, ``compute_size``, ``sinc_table``,
+``wavelet_deriv``, ``source_geometry``, ``receiver_geometry``,
+``rand_subspace``, ``extract_sub``, ``laplac_forward``): the package itself,
+or a CPU restatement with the same functions, which gives bit-identical
+arrays.  This module itself is plain numpy.
 """
 from __future__ import annotations
 
@@ -93,11 +98,12 @@ CONFIGS = {
 }
 
 
-def prepare_shot(born, name: str = "c2", nt: int | None = None,
+def prepare_shot(geo, name: str = "c2", nt: int | None = None,
                  n: int | None = None, nbound: int | None = None,
                  shot: int = 0) -> dict:
     """Propagator inputs for shot ``shot`` of configuration ``name`` (shot 0
-    at the model centre, others offset along x on a 20 m lattice)."""
+    at the model centre, others offset along x on a 20 m lattice); ``geo``
+    provides the host geometry (see the module docstring)."""
     cfg = dict(CONFIGS[name])
     if n is not None:
         cfg["n"] = n
@@ -107,42 +113,36 @@ def prepare_shot(born, name: str = "c2", nt: int | None = None,
     vel = cfg["model"](n)
     dt_data = 0.001
     nt_data = nt if nt is not None else cfg["nt"]
-    dt, nt_fd = born.calc_stability(float(vel.max()), d, dt_data, nt_data)
+    dt, nt_fd = geo.calc_stability(float(vel.max()), d, dt_data, nt_data)
     jt = int(round(dt_data / dt))
     fat = 4
-    nc = born.compute_size(n, nb, fat)
+    nc = geo.compute_size(n, nb, fat)
     o_c = -d * (nb + fat)
     o = (o_c, o_c, o_c)
     dd = (d, d, d)
-    table = born.sinc_table(jt, 8)
+    table = geo.sinc_table(jt, 8)
     nt_big = nt_data + 8
-    wav = born.wavelet_deriv(ricker(nt_data, dt_data, cfg["f"]), dt_data)
+    wav = geo.wavelet_deriv(ricker(nt_data, dt_data, cfg["f"]), dt_data)
     mid = (n // 2) * d
     sx = mid + 20.0 * (((shot * 7) % 11) - 5 if shot else 0)
-    locs_s, src = born.source_geometry(sx, mid, cfg["src_depth"], o, dd, nc,
-                                       nc, wav, nt_big)
+    locs_s, src = geo.source_geometry(sx, mid, cfg["src_depth"], o, dd, nc,
+                                      nc, wav, nt_big)
     seed = int(locs_s[3] % 10000)
     shape = (nc, nc, nc)
-    vrand = born.rand_subspace(vel, (0., 0., 0.), dd, float(vel.max()), seed,
-                               (nb, nb, nb), dt, shape, o, dd)
-    vnone = born.rand_subspace(vel, (0., 0., 0.), dd, float(vel.max()), seed,
-                               (0, 0, 0), dt, shape, o, dd)
+    vrand = geo.rand_subspace(vel, (0., 0., 0.), dd, float(vel.max()), seed,
+                              (nb, nb, nb), dt, shape, o, dd)
+    vnone = geo.rand_subspace(vel, (0., 0., 0.), dd, float(vel.max()), seed,
+                              (0, 0, 0), dt, shape, o, dd)
     nr, dr = cfg["rec"]
     r0 = mid - dr * (nr // 2)
-    locs_r = born.receiver_geometry(nr, nr, r0, dr, r0, dr, cfg["rec_depth"],
-                                    o, dd, nc, nc)
+    locs_r = geo.receiver_geometry(nr, nr, r0, dr, r0, dr, cfg["rec_depth"],
+                                   o, dd, nc, nc)
     rng = np.random.default_rng(SEEDS["data"])
     rec = np.zeros((nr * nr, nt_big), np.float32)
     rec[:, 4:4 + nt_data] = 1e-3 * rng.standard_normal((nr * nr, nt_data))
     # model-grid reflectivity -> compute-grid window -> z first difference
-    refl_m = reflectivity(vel)
-    sub = np.zeros(shape, np.float32)
-    born.lib().born_extract_sub(born.fptr(refl_m), n, n, n, born.fptr(sub),
-                                nc, nc, nc, -(nb + fat), -(nb + fat),
-                                -(nb + fat))
-    refl = np.zeros(shape, np.float32)
-    born.lib().born_laplac_forward(0, born.fptr(sub), born.fptr(refl), nc, nc,
-                                   nc)
+    sub = geo.extract_sub(reflectivity(vel), shape, (-(nb + fat),) * 3)
+    refl = geo.laplac_forward(sub)
     return dict(shape=shape, d=d, nt=nt_fd, jts=jt, jtd=jt, nt_big=nt_big,
                 table_s=table, table_d=table, locs_s=locs_s, src=src,
                 vel1=vrand, vel2=vnone, locs_r=locs_r, rec_nx=nr, rec_ny=nr,

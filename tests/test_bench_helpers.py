@@ -51,3 +51,20 @@ def test_peak_lookup_and_fallback(bench, tmp_path, monkeypatch):
 def test_aggregate_rate_counts_all_ranks(bench):
     # 2 ranks, 3 steps of 1e9 cell-updates each in 1.5 s: 4 G cell-updates/s
     assert bench.aggregate_rate(1e9, 3, 1500.0, 2) == pytest.approx(4.0, rel=1e-3)
+
+
+def test_reference_arm_inputs_equal_gpu_arm_inputs(bench, born, po):
+    """The reference arm builds the shot from the oracle's geometry (so it
+    loads no product library); the arrays equal those the GPU arm builds
+    with the product's host geometry, bit for bit (reduced c2 model)."""
+    import numpy as np
+    wl = bench.workload_module()
+    a = wl.prepare_shot(born, "c2", nt=30, n=48)
+    b = wl.prepare_shot(po.Geometry(), "c2", nt=30, n=48)
+    for k, v in a.items():
+        if isinstance(v, np.ndarray):
+            assert np.array_equal(v, b[k]), k
+        else:
+            assert v == b[k], k
+    # both arms print the same config object
+    assert bench.arm_config(a, "f32", 1) == bench.arm_config(b, "f32", 1)
