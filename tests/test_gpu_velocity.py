@@ -84,8 +84,10 @@ def test_device_velocity_tapered_bound(born):
     assert np.all(v > 0)
     # outside the bands: the plain model
     assert np.allclose(v[~band], val[~band], rtol=1e-6)
-    # cells that found no accepted draw keep 0.999 of the bound
-    fallback = band & np.isclose(v, 0.999 * bound, rtol=1e-6)
+    # cells that found no accepted draw in 64 keep 0.999 of the bound
+    # (val >= bound) or their value (val < bound); few do
+    fallback = band & (np.isclose(v, 0.999 * bound, rtol=1e-6) |
+                       np.isclose(v, val, rtol=1e-7))
     assert fallback.sum() < 0.01 * band.sum()
     acc = band & ~fallback
     u = (v[acc] / val[acc] - 1.0) / (1.3 * dist[acc]) + 0.5 + 0.49 * dist[acc]
