@@ -259,9 +259,39 @@ int born_op_sizes(const born_op *op, long long *model_n, long long *data_n,
                   int *nt_fd, float *dt_fd);
 int born_op_forward(born_op *op, int add, const float *model, float *data);
 int born_op_adjoint(born_op *op, int add, float *model, const float *data);
-/* FP64 dot product of two device float vectors (block partials in double). */
+/* FP64 dot product of two device float vectors (block partials in double),
+ * the dot of hypercube_float (hypercube_float.cc:120-130) on the device. */
 int born_dot_f64(born_op *op, const float *a, const float *b, long long n,
                  double *out);
+
+/* Device vectors of n floats on the operator's device, and the vector
+ * algebra of the reference's hypercube_float (the my_vector that
+ * rtm_zero_op and lin_solver use, base/my_vector.h:7-91), ordered on the
+ * operator's stream: factors are double, each element is formed in double
+ * and stored as float, as hypercube_float does.  csrc/born_my_operator.h
+ * wraps them in a my_vector subclass so that the reference's lin_solver /
+ * cgstep drive the operator unchanged.
+ *   create:    x = 0 (cudaMalloc);  destroy: waits for the stream, frees
+ *   fill:      x = val                    (hypercube_float.cc:50-52)
+ *   scale:     x = x r                    (hypercube_float.h:25-27)
+ *   scale_add: x = x a + y b              (hypercube_float.cc:213-222)
+ *   lincomb:   x = y a + z b              (hypercube_float.cc:140-151)
+ *   add:       x = x + y  (float add)     (hypercube_float.cc:223-228)
+ *   copy, upload (host -> device), download (device -> host); the two host
+ *   copies return when done. */
+int born_vec_create(born_op *op, long long n, float **out);
+int born_vec_destroy(born_op *op, float *x);
+int born_vec_fill(born_op *op, float *x, long long n, double val);
+int born_vec_scale(born_op *op, float *x, long long n, double r);
+int born_vec_scale_add(born_op *op, float *x, double a, const float *y,
+                       double b, long long n);
+int born_vec_lincomb(born_op *op, float *x, double a, const float *y,
+                     double b, const float *z, long long n);
+int born_vec_add(born_op *op, float *x, const float *y, long long n);
+int born_vec_copy(born_op *op, float *dst, const float *src, long long n);
+int born_vec_upload(born_op *op, float *dst, const float *host, long long n);
+int born_vec_download(born_op *op, float *host, const float *src,
+                      long long n);
 /* Least squares by Claerbout's CG (lin_solver.cc:104-132, cgstep.cc:11-54):
  * model (device, in: starting model, out: solution); resid (host, niter+1
  * doubles, nullable) receives rr.rr before and after every iteration. */

@@ -46,10 +46,18 @@ def build_ref(force: bool = False) -> str | None:
     """Compile the reference CPU path when its sources are present here."""
     if not REF_SRC or not os.path.isdir(os.path.join(REF_SRC, "base")):
         return REF_SO if os.path.exists(REF_SO) else None
-    if force or not os.path.exists(REF_SO):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"],
-                       check=True)
+    # make rebuilds only what is older than its sources
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"] +
+                   (["-B"] if force else []), check=True)
     return REF_SO
+
+
+def ref_program(name: str) -> str | None:
+    """A program of oracle/_ref built on the reference's own sources (see
+    the Makefile), or None where it was never built."""
+    build_ref()
+    path = os.path.join(HERE, "_ref", name)
+    return path if os.path.exists(path) else None
 
 
 REF_GEOM_SO = os.path.join(HERE, "_ref", "libref_geom.so")

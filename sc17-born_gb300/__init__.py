@@ -124,6 +124,18 @@ _SIGS = {
                                C.POINTER(C.c_double)]),
     "born_cg_solve": (C.c_int, [_vp, _vp, _vp, C.c_int,
                                 C.POINTER(C.c_double)]),
+    "born_vec_create": (C.c_int, [_vp, C.c_longlong, C.POINTER(_vp)]),
+    "born_vec_destroy": (C.c_int, [_vp, _vp]),
+    "born_vec_fill": (C.c_int, [_vp, _vp, C.c_longlong, C.c_double]),
+    "born_vec_scale": (C.c_int, [_vp, _vp, C.c_longlong, C.c_double]),
+    "born_vec_scale_add": (C.c_int, [_vp, _vp, C.c_double, _vp, C.c_double,
+                                     C.c_longlong]),
+    "born_vec_lincomb": (C.c_int, [_vp, _vp, C.c_double, _vp, C.c_double,
+                                   _vp, C.c_longlong]),
+    "born_vec_add": (C.c_int, [_vp, _vp, _vp, C.c_longlong]),
+    "born_vec_copy": (C.c_int, [_vp, _vp, _vp, C.c_longlong]),
+    "born_vec_upload": (C.c_int, [_vp, _vp, _fp, C.c_longlong]),
+    "born_vec_download": (C.c_int, [_vp, _fp, _vp, C.c_longlong]),
     "born_dot_f64_noalloc": (C.c_int, [_vp, _vp, C.c_longlong,
                                        C.POINTER(C.c_double), _vp]),
     # host geometry (csrc/born_host.h)

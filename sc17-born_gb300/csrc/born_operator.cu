@@ -211,6 +211,29 @@ __global__ void k_add(float *x, const float *y, long long n) {
     x[i] = __fadd_rn(x[i], y[i]);
 }
 
+// x = y sc1 + z sc2 in double, stored as float (the four-argument
+// hypercube_float::scale_add, hypercube_float.cc:140-151)
+__global__ void k_lincomb(float *x, double sc1, const float *y, double sc2,
+                          const float *z, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = (float)((double)y[i] * sc1 + (double)z[i] * sc2);
+}
+
+// x = x r in double, stored as float (hypercube_float.h:25-27)
+__global__ void k_scale(float *x, double r, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = (float)((double)x[i] * r);
+}
+
+// x = (float) val (hypercube_float.cc:50-52)
+__global__ void k_fill(float *x, float val, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = val;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -515,6 +538,123 @@ int born_dot_f64(born_op *op, const float *a, const float *b, long long n,
                  double *out) {
   if (!op || !a || !b || !out || n < 0) return BORN_EINVAL;
   return op_dot(op, a, b, n, out);
+}
+
+// ---- device vectors for host code that holds them in my_vector objects
+// (born_my_operator.h); every call is ordered on the operator's stream ----
+
+namespace {
+int vec_ready(born_op *op, long long n) {
+  if (!op || n < 0) return BORN_EINVAL;
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess) return BORN_ECUDA;
+  if (dev != op->h->device && cudaSetDevice(op->h->device) != cudaSuccess)
+    return born_fail(op->h, BORN_ECUDA, "cannot select the operator's device");
+  return BORN_OK;
+}
+int vec_launched(born_op *op) {
+  op->h->launches++;
+  OPCK(op, cudaGetLastError());
+  return BORN_OK;
+}
+}  // namespace
+
+int born_vec_create(born_op *op, long long n, float **out) {
+  int rc = vec_ready(op, n);
+  if (rc) return rc;
+  if (!out) return BORN_EINVAL;
+  *out = nullptr;
+  float *x = nullptr;
+  if (cudaMalloc(&x, (size_t)std::max<long long>(n, 1) * 4) != cudaSuccess)
+    return born_fail(op->h, BORN_ENOMEM, "born_vec_create: %lld floats", n);
+  if (cudaMemsetAsync(x, 0, (size_t)n * 4, op->h->stream) != cudaSuccess) {
+    cudaFree(x);
+    return born_fail(op->h, BORN_ECUDA, "born_vec_create: clear failed");
+  }
+  *out = x;
+  return BORN_OK;
+}
+
+int born_vec_destroy(born_op *op, float *x) {
+  int rc = vec_ready(op, 0);
+  if (rc) return rc;
+  if (!x) return BORN_OK;
+  // work queued on the stream may still read or write x
+  OPCK(op, cudaStreamSynchronize(op->h->stream));
+  OPCK(op, cudaFree(x));
+  return BORN_OK;
+}
+
+int born_vec_fill(born_op *op, float *x, long long n, double val) {
+  int rc = vec_ready(op, n);
+  if (rc || n == 0) return rc;
+  if (!x) return BORN_EINVAL;
+  k_fill<<<grid_for(n), kThreads, 0, op->h->stream>>>(x, (float)val, n);
+  return vec_launched(op);
+}
+
+int born_vec_scale(born_op *op, float *x, long long n, double r) {
+  int rc = vec_ready(op, n);
+  if (rc || n == 0) return rc;
+  if (!x) return BORN_EINVAL;
+  k_scale<<<grid_for(n), kThreads, 0, op->h->stream>>>(x, r, n);
+  return vec_launched(op);
+}
+
+int born_vec_scale_add(born_op *op, float *x, double a, const float *y,
+                       double b, long long n) {
+  int rc = vec_ready(op, n);
+  if (rc || n == 0) return rc;
+  if (!x || !y) return BORN_EINVAL;
+  k_scale_add<<<grid_for(n), kThreads, 0, op->h->stream>>>(x, a, y, b, n);
+  return vec_launched(op);
+}
+
+int born_vec_lincomb(born_op *op, float *x, double a, const float *y,
+                     double b, const float *z, long long n) {
+  int rc = vec_ready(op, n);
+  if (rc || n == 0) return rc;
+  if (!x || !y || !z) return BORN_EINVAL;
+  k_lincomb<<<grid_for(n), kThreads, 0, op->h->stream>>>(x, a, y, b, z, n);
+  return vec_launched(op);
+}
+
+int born_vec_add(born_op *op, float *x, const float *y, long long n) {
+  int rc = vec_ready(op, n);
+  if (rc || n == 0) return rc;
+  if (!x || !y) return BORN_EINVAL;
+  k_add<<<grid_for(n), kThreads, 0, op->h->stream>>>(x, y, n);
+  return vec_launched(op);
+}
+
+int born_vec_copy(born_op *op, float *dst, const float *src, long long n) {
+  int rc = vec_ready(op, n);
+  if (rc || n == 0) return rc;
+  if (!dst || !src) return BORN_EINVAL;
+  OPCK(op, cudaMemcpyAsync(dst, src, (size_t)n * 4, cudaMemcpyDeviceToDevice,
+                           op->h->stream));
+  return BORN_OK;
+}
+
+int born_vec_upload(born_op *op, float *dst, const float *host, long long n) {
+  int rc = vec_ready(op, n);
+  if (rc || n == 0) return rc;
+  if (!dst || !host) return BORN_EINVAL;
+  OPCK(op, cudaMemcpyAsync(dst, host, (size_t)n * 4, cudaMemcpyHostToDevice,
+                           op->h->stream));
+  OPCK(op, cudaStreamSynchronize(op->h->stream));
+  return BORN_OK;
+}
+
+int born_vec_download(born_op *op, float *host, const float *src,
+                      long long n) {
+  int rc = vec_ready(op, n);
+  if (rc || n == 0) return rc;
+  if (!host || !src) return BORN_EINVAL;
+  OPCK(op, cudaMemcpyAsync(host, src, (size_t)n * 4, cudaMemcpyDeviceToHost,
+                           op->h->stream));
+  OPCK(op, cudaStreamSynchronize(op->h->stream));
+  return BORN_OK;
 }
 
 // Claerbout CG (lin_solver.cc:104-132 with cgstep.cc:11-54):
