@@ -27,6 +27,10 @@ Multi-GPU: shots are independent, so N ranks run N shots (weak scaling);
 each step ends with the images summed over the ranks (one NCCL all-reduce,
 the only exchange an RTM over shots needs).
 
+``--adjoint exact`` times c2 as its configuration states it instead: the
+exact linearised Born pair, the adjoint rebuilding the background from
+checkpoints every 50 steps (per-phase times and bytes in the line).
+
 Other configurations print their own line:
   --config c3  one 624^3 shot (512^3 model at 8 m, jt = 2, nt = 2999) per
                level storage (--storage f32,f32fma,bf16,f16; default
@@ -542,6 +546,138 @@ def e2e_measure(born, case, args, dev, cells_per_step, world):
             "api": "gpu_funcs_3d.h entry points, pinned host buffers"}
 
 
+def run_exact(args):
+    """c2 as its configuration states it: the exact linearised Born pair,
+    born_lin_forward along the reflectivity and born_lin_adjoint of the
+    traces it made (the source wavefield rebuilt from checkpoints every
+    --ckpt steps), device-resident; one step = one forward + one adjoint of
+    the shot, 2 * N_interior * nt cell-updates as in the headline line.
+
+    Algorithmic bytes per interior cell and FD step: forward 32 (s and r:
+    two levels each, velocity, reflectivity in; two levels out); adjoint 64 =
+    checkpointing sweep of the background 16 + segment recompute storing
+    A s 20 + adjoint step 28 (w: two levels, A s, velocity, image in; w and
+    image out); plus 32 B per grid cell per segment for the checkpoint
+    stores and restores (two levels each way) and 12 for the final division
+    by v^2 dt^2."""
+    import torch
+    born = package()
+    born.lib()
+    wl = workload_module()
+    case = wl.prepare_shot(born, args.config, nt=args.nt, n=args.model_n)
+    nz, ny, nx = case["shape"]
+    nt, jt = case["nt"], case["jts"]
+    n_int = wl.interior_cells(case["shape"])
+    n123 = nx * ny * nz
+    interval = args.ckpt
+    nseg = (nt + interval - 1) // interval
+    prop = born.Gb300Prop(0)
+    prop.createSpace(case["d"], case["d"], case["d"], 50.0, 0.0005, 0.0005,
+                     nx, ny, nz)
+    prop.transferSincTableS(8, jt, case["table_s"])
+    prop.transferSincTableD(8, jt, case["table_d"])
+    prop.transferSourceFunc(9, case["nt_big"], case["locs_s"], case["src"])
+    prop.transferVelFunc1(nx, ny, nz, case["vel1"])
+    prop.transferVelFunc2(nx, ny, nz, case["vel2"])
+    rec = np.zeros_like(case["rec_in"])
+    prop.transferReceiverFunc(case["rec_nx"], case["rec_ny"], case["nt_big"],
+                              case["locs_r"], rec)
+    prop.check(prop.lib.born_set_reflectivity(prop.h, born.fptr(case["refl"])))
+    stream = torch.cuda.ExternalStream(prop.stream, device=0)
+
+    def step(ev=None):
+        prop.zero_traces()
+        if ev:
+            ev[0].record(stream)
+        prop.lin_forward_device(jt, nt)
+        if ev:
+            ev[1].record(stream)
+        prop.lin_adjoint_device(jt, nt, interval)
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    prop.synchronize()
+    launches0 = prop.launches
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(3)]
+           for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    with Clocks(0) as clk:
+        start = torch.cuda.Event(enable_timing=True)
+        stop = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for k in range(args.steps):
+            step(evs[k])
+        stop.record(stream)
+        prop.synchronize()
+        torch.cuda.synchronize()
+    launches = prop.launches - launches0
+    t_ms = start.elapsed_time(stop)
+    fwd_ms = sum(e[0].elapsed_time(e[1]) for e in evs) / args.steps
+    adj_ms = sum(e[1].elapsed_time(e[2]) for e in evs) / args.steps
+    # one more adjoint with its phases timed (events at phase boundaries)
+    prop.time_phases(True)
+    prop.zero_traces()
+    prop.lin_forward_device(jt, nt)
+    prop.lin_adjoint_device(jt, nt, interval)
+    prop.synchronize()
+    sweep_ms, recomp_ms, rev_ms, div_ms = prop.phase_times()
+    prop.time_phases(False)
+    cells = 2 * n_int * nt
+    value = cells * args.steps / (t_ms / 1e3) / 1e9
+    algo = n_int * (32 + 64) * nt + n123 * (32 * nseg + 12)
+    peak, peak_kind = measured_peak()
+    phases = {
+        "lin_forward_ms": round(fwd_ms, 2), "lin_adjoint_ms": round(adj_ms, 2),
+        "adjoint_sweep_ms": round(sweep_ms, 2),
+        "adjoint_recompute_ms": round(recomp_ms, 2),
+        "adjoint_reverse_ms": round(rev_ms, 2),
+        "adjoint_division_ms": round(div_ms, 3),
+        "lin_forward_GBps": round(32 * n_int * nt / (fwd_ms / 1e3) / 1e9, 1),
+        "sweep_GBps": round(16 * n_int * nt / (sweep_ms / 1e3) / 1e9, 1),
+        "recompute_GBps": round(20 * n_int * nt / (recomp_ms / 1e3) / 1e9, 1),
+        "reverse_GBps": round(28 * n_int * nt / (rev_ms / 1e3) / 1e9, 1)}
+    # roofline of the largest single kernel family by time
+    fams = {"forward": (fwd_ms, 32, "step_kernel<born_lin> (s and r, "
+                        "scattering source m A s)"),
+            "reverse": (rev_ms, 28, "step_kernel<born_adj> (w step, image "
+                        "+= (A s) w)"),
+            "recompute": (recomp_ms, 20, "step_kernel<model> (background "
+                          "step storing A s)"),
+            "sweep": (sweep_ms, 16, "step_kernel<model> (background step)")}
+    top = max(fams, key=lambda k: fams[k][0])
+    ms_top, bpc, kname = fams[top]
+    achieved = bpc * n_int / (ms_top / nt / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": None, "kernel": kname, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": bpc * n_int,
+                "avg_launch_ms": round(ms_top / nt, 4),
+                "whole_step_GBps": round(algo / (t_ms / args.steps / 1e3) /
+                                         1e9, 1)}
+    line = {"metric": "Gcell-updates/s Born fwd+adj (exact pair, "
+                      "checkpointed adjoint)",
+            "value": round(value, 3), "unit": "Gcell-updates/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(t_ms / args.steps, 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded, shapes of the config)",
+            "config": {"workload": f"{case['name']}: exact linearised Born "
+                       f"forward + adjoint, compute grid {nx}x{ny}x{nz}, "
+                       f"nt={nt}, background checkpointed every {interval} "
+                       "steps", "grid": [nz, ny, nx], "nt": nt,
+                       "ckpt_interval": interval, "interior_cells": n_int,
+                       "l2": "inputs larger than L2"},
+            "algorithmic_bytes_per_step": int(algo),
+            "roofline": roofline, "phases": phases,
+            "checkpoint_bytes": int(2 * nseg * n123 * 4),
+            "segment_bytes": int(interval * n123 * 4),
+            "clocks": clk.summary(), "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_batched(args):
     """c4: batched multi-shot RTM (source propagation + adjoint of every
     shot, one launch per step for all shots, time loops as CUDA graphs)
@@ -811,6 +947,13 @@ def main():
                     help="smaller model edge (profiling cases)")
     ap.add_argument("--nt", type=int, default=None,
                     help="fewer time steps (profiling cases)")
+    ap.add_argument("--adjoint", default="reference",
+                    choices=["reference", "exact"],
+                    help="c1/c2: the reference's random-boundary RTM pair "
+                         "(default) or the exact linearised pair with the "
+                         "checkpointed adjoint")
+    ap.add_argument("--ckpt", type=int, default=50,
+                    help="--adjoint exact: checkpoint interval (steps)")
     ap.add_argument("--tile", type=int, default=-1)
     ap.add_argument("--zseg", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -841,6 +984,8 @@ def main():
         return run_batched(args)
     if args.config == "c5":
         return run_lsrtm(args)
+    if args.adjoint == "exact":
+        return run_exact(args)
     return run_gpu_arm(args)
 
 

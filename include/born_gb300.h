@@ -200,6 +200,15 @@ int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out);
 int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
                      float *model_out);
 
+/* Phase timing of born_lin_adjoint (off by default): with enable != 0 the
+ * loop records a CUDA event at every phase boundary on the handle's stream
+ * and, at its end, waits for them; born_phase_times then gives the last
+ * call's ms in ms[0..3] = forward sweep (with the checkpoint stores),
+ * segment restores and recompute (storing A s), reverse adjoint steps,
+ * final division by v^2 dt^2. */
+int born_time_phases(born_handle *h, int enable);
+int born_phase_times(const born_handle *h, float *ms, int n);
+
 /* Device results and state transfers (host arrays of n1*n2*n3 floats, or
  * npts*nt_big for traces) */
 int born_get_image(born_handle *h, float *img_out);

@@ -95,6 +95,8 @@ _SIGS = {
     "born_autotune": (C.c_int, [_vp, C.c_int]),
     "born_tuned_config": (C.c_int, [_vp, C.c_int, _ip, _fp]),
     "born_loop_tile_ms": (C.c_int, [_vp, C.c_int, _fp, C.c_int]),
+    "born_time_phases": (C.c_int, [_vp, C.c_int]),
+    "born_phase_times": (C.c_int, [_vp, _fp, C.c_int]),
     "born_selftest_wait_timeout": (C.c_int, [_vp]),
     "born_stream_mix_gbs": (C.c_int, [C.c_int, C.c_int, C.c_longlong,
                                       C.c_int, _fp]),
@@ -444,6 +446,26 @@ class Gb300Prop(Handle):
         self.check(self.lib.born_lin_adjoint(self.h, jt, nt, interval,
                                              fptr(out)))
         return out
+
+    def lin_adjoint_device(self, jt, nt, interval=50):
+        """born_lin_adjoint on the device traces, result left in the device
+        image (no host copy)."""
+        self.check(self.lib.born_lin_adjoint(self.h, jt, nt, interval, None))
+
+    def lin_forward_device(self, jt, nt):
+        """born_lin_forward along the device reflectivity, traces left on
+        the device (accumulated onto the current device traces)."""
+        self.check(self.lib.born_lin_forward(self.h, jt, nt, None))
+
+    def time_phases(self, enable=True):
+        self.check(self.lib.born_time_phases(self.h, int(enable)))
+
+    def phase_times(self):
+        """ms of the last born_lin_adjoint's phases: forward sweep,
+        recompute, reverse adjoint steps, division."""
+        out = (C.c_float * 4)()
+        self.check(self.lib.born_phase_times(self.h, out, 4))
+        return [float(v) for v in out]
 
     def get_image(self):
         out = np.empty(self.shape, np.float32)

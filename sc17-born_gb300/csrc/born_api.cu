@@ -1206,6 +1206,36 @@ int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
 }
 
 namespace {
+// CUDA events recorded one after another on the handle's stream (none when
+// count is 0); elapsed() waits for the later event.
+struct PhaseEvents {
+  born_handle *h;
+  std::vector<cudaEvent_t> ev;
+  int next = 0;
+  PhaseEvents(born_handle *hh, int count) : h(hh) {
+    for (int i = 0; i < count; ++i) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreate(&e) != cudaSuccess) break;
+      ev.push_back(e);
+    }
+  }
+  ~PhaseEvents() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
+  }
+  int record() {
+    if (ev.empty()) return BORN_OK;
+    if (next >= (int)ev.size())
+      return fail(h, BORN_ECUDA, "phase timing: out of events");
+    CK(h, cudaEventRecord(ev[next++], h->stream));
+    return BORN_OK;
+  }
+  int elapsed(int a, int b, float *ms) {
+    CK(h, cudaEventSynchronize(ev[b]));
+    CK(h, cudaEventElapsedTime(ms, ev[a], ev[b]));
+    return BORN_OK;
+  }
+};
+
 int ensure_levels(born_handle *h, float **buf, size_t *have, size_t levels) {
   if (*have >= levels) return BORN_OK;
   cudaFree(*buf);
@@ -1237,6 +1267,10 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
   if (!rc) rc = ensure_levels(h, &h->gbuf, &h->gbuf_levels, (size_t)interval);
   if (rc) return rc;
   const float scale = 1 / (float)jt;
+  // optional phase timing: one event at every phase boundary on the stream
+  PhaseEvents pe(h, h->time_phases ? 2 * nseg + 3 : 0);
+  rc = pe.record();
+  if (rc) return rc;
   auto model_step = [&](float *sp0, float *sp1, int it, float *g) {
     const int id = it / jt, ii = it - id * jt;
     StepParams p;
@@ -1265,6 +1299,8 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
     if (rc) return rc;
     std::swap(sp0, sp1);
   }
+  rc = pe.record();
+  if (rc) return rc;
   // reverse sweep
   CK(h, cudaMemsetAsync(h->r0, 0, bytes, h->stream));
   CK(h, cudaMemsetAsync(h->r1, 0, bytes, h->stream));
@@ -1284,6 +1320,8 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
       if (rc) return rc;
       std::swap(a0, a1);
     }
+    rc = pe.record();
+    if (rc) return rc;
     for (int it = t1 - 1; it >= t0; --it) {
       const int id = it / jt, ii = it - id * jt;
       StepParams p;
@@ -1298,9 +1336,28 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
       if (rc) return rc;
       std::swap(wp0, wp1);
     }
+    rc = pe.record();
+    if (rc) return rc;
   }
   CK(h, born::launch_divide(h->img, h->vel2, h->img, h->n123, h->stream));
   h->launches++;
+  rc = pe.record();
+  if (!rc && h->time_phases) {
+    // events: start, end of sweep, then (recompute end, reverse end) per
+    // segment, then the end of the division
+    float ms[4] = {0.f, 0.f, 0.f, 0.f};
+    rc = pe.elapsed(0, 1, &ms[0]);
+    for (int k = 0; !rc && k < nseg; ++k) {
+      float a = 0.f, b = 0.f;
+      rc = pe.elapsed(1 + 2 * k, 2 + 2 * k, &a);
+      if (!rc) rc = pe.elapsed(2 + 2 * k, 3 + 2 * k, &b);
+      ms[1] += a;
+      ms[2] += b;
+    }
+    if (!rc) rc = pe.elapsed(2 * nseg + 1, 2 * nseg + 2, &ms[3]);
+    for (int k = 0; k < 4; ++k) h->phase_ms[k] = ms[k];
+  }
+  if (rc) return rc;
   if (model_out) {
     CK(h, cudaMemcpyAsync(model_out, h->img, bytes, cudaMemcpyDeviceToHost,
                           h->stream));
@@ -1418,6 +1475,18 @@ int born_loop_tile_ms(const born_handle *h, int mode, float *ms, int n) {
   for (int c = 0; c < n; ++c)
     ms[c] = c < born_handle::kMaxTileCfgs ? h->loop_ms[h->storage][mode][c]
                                           : 0.f;
+  return BORN_OK;
+}
+
+int born_time_phases(born_handle *h, int enable) {
+  if (!h) return BORN_EINVAL;
+  h->time_phases = enable != 0;
+  return BORN_OK;
+}
+
+int born_phase_times(const born_handle *h, float *ms, int n) {
+  if (!h || !ms || n < 0) return BORN_EINVAL;
+  for (int k = 0; k < n && k < 4; ++k) ms[k] = h->phase_ms[k];
   return BORN_OK;
 }
 

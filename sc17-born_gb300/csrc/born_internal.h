@@ -136,6 +136,11 @@ struct born_handle {
   // exact linearised adjoint: checkpoints and the per-segment A s buffer
   float *ckpt = nullptr, *gbuf = nullptr;
   size_t ckpt_levels = 0, gbuf_levels = 0;
+  // phase times (ms) of the last born_lin_adjoint when timing is enabled:
+  // forward sweep with checkpoint stores, segment restores and recompute,
+  // reverse adjoint steps, final division (born_phase_times)
+  bool time_phases = false;
+  float phase_ms[4] = {};
 };
 
 

@@ -146,3 +146,25 @@ def test_autograd_function_uses_adjoint_kernel(gpu, po):
     dd = float(np.dot(r.ravel().astype(np.float64), jq.ravel()))
     gq = float(np.dot(m.grad.numpy().ravel().astype(np.float64), q.ravel()))
     assert abs(dd - gq) <= 1e-5 * abs(dd)
+
+
+def test_lin_adjoint_phase_timing(gpu, po):
+    """Phase timing (born_time_phases) records events only: the gradient is
+    bit-identical with it on, and the four phase times are positive and add
+    up to no more than the call's own time."""
+    import time
+    c = case(po, seed=83, nt=120)
+    g = gpu.Gb300Prop()
+    setup(g, c)
+    rng = np.random.default_rng(5)
+    tr = rng.standard_normal(c["rec_in"].shape).astype(np.float32)
+    want = g.lin_adjoint(c["jts"], c["nt"], tr, interval=25)
+    g.time_phases(True)
+    t0 = time.perf_counter()
+    got = g.lin_adjoint(c["jts"], c["nt"], tr, interval=25)
+    wall_ms = 1e3 * (time.perf_counter() - t0)
+    ms = g.phase_times()
+    g.time_phases(False)
+    assert np.array_equal(got, want)
+    assert all(v > 0 for v in ms), ms
+    assert sum(ms) <= wall_ms, (ms, wall_ms)
