@@ -554,12 +554,13 @@ def run_exact(args):
     the shot, 2 * N_interior * nt cell-updates as in the headline line.
 
     Algorithmic bytes per interior cell and FD step: forward 32 (s and r:
-    two levels each, velocity, reflectivity in; two levels out); adjoint 64 =
-    checkpointing sweep of the background 16 + segment recompute storing
-    A s 20 + adjoint step 28 (w: two levels, A s, velocity, image in; w and
-    image out); plus 32 B per grid cell per segment for the checkpoint
-    stores and restores (two levels each way) and 12 for the final division
-    by v^2 dt^2."""
+    two levels each, velocity, reflectivity in; two levels out); adjoint 48
+    = segment recompute storing A s 20 + adjoint step 28 (w: two levels,
+    A s, velocity, image in; w and image out), plus 16 for a checkpointing
+    sweep of the background when the forward's checkpoints cannot be reused
+    (the line says which); plus 16 B per grid cell per segment for the
+    checkpoint stores and 16 for their restores (two levels each) and 12 for
+    the final division by v^2 dt^2."""
     import torch
     born = package()
     born.lib()
@@ -583,6 +584,7 @@ def run_exact(args):
     prop.transferReceiverFunc(case["rec_nx"], case["rec_ny"], case["nt_big"],
                               case["locs_r"], rec)
     prop.check(prop.lib.born_set_reflectivity(prop.h, born.fptr(case["refl"])))
+    prop.check(prop.lib.born_set_checkpoint_interval(prop.h, interval))
     stream = torch.cuda.ExternalStream(prop.stream, device=0)
 
     def step(ev=None):
@@ -623,10 +625,12 @@ def run_exact(args):
     prop.lin_adjoint_device(jt, nt, interval)
     prop.synchronize()
     sweep_ms, recomp_ms, rev_ms, div_ms = prop.phase_times()
+    reused = bool(prop.lib.born_checkpoints_reused(prop.h))
     prop.time_phases(False)
     cells = 2 * n_int * nt
     value = cells * args.steps / (t_ms / 1e3) / 1e9
-    algo = n_int * (32 + 64) * nt + n123 * (32 * nseg + 12)
+    algo = n_int * (32 + 48 + (0 if reused else 16)) * nt + \
+        n123 * (32 * nseg + 12)
     peak, peak_kind = measured_peak()
     phases = {
         "lin_forward_ms": round(fwd_ms, 2), "lin_adjoint_ms": round(adj_ms, 2),
@@ -635,7 +639,9 @@ def run_exact(args):
         "adjoint_reverse_ms": round(rev_ms, 2),
         "adjoint_division_ms": round(div_ms, 3),
         "lin_forward_GBps": round(32 * n_int * nt / (fwd_ms / 1e3) / 1e9, 1),
-        "sweep_GBps": round(16 * n_int * nt / (sweep_ms / 1e3) / 1e9, 1),
+        "checkpoints_from_forward": reused,
+        "sweep_GBps": (round(16 * n_int * nt / (sweep_ms / 1e3) / 1e9, 1)
+                       if not reused else None),
         "recompute_GBps": round(20 * n_int * nt / (recomp_ms / 1e3) / 1e9, 1),
         "reverse_GBps": round(28 * n_int * nt / (rev_ms / 1e3) / 1e9, 1)}
     # roofline of the largest single kernel family by time

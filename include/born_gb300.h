@@ -196,9 +196,23 @@ int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out);
 /* Exact adjoint of born_lin_forward: reads the device traces, returns the
  * model-space gradient (n1*n2*n3) in model_out (also left in the device
  * image).  The background is checkpointed every `interval` steps (two levels
- * per checkpoint) and recomputed segment by segment. */
+ * per checkpoint) and recomputed segment by segment.  The checkpoints come
+ * from a forward sweep of the background, which is skipped when the
+ * checkpoints already held are those of the same background: stored by
+ * born_lin_forward (every born_set_checkpoint_interval steps, 50 by
+ * default) or by an earlier adjoint, with vel2, the source points and
+ * traces, the source sinc table and the grid unchanged since and the same
+ * jt, nt and interval.  The result does not depend on which way the
+ * checkpoints were made (the background step is the same arithmetic). */
 int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
                      float *model_out);
+/* Checkpoint interval at which born_lin_forward stores the background (0:
+ * it stores none; 2 * ceil(nt / interval) levels of n1*n2*n3 floats are
+ * kept per handle). */
+int born_set_checkpoint_interval(born_handle *h, int interval);
+/* 1 when the last born_lin_adjoint reused checkpoints instead of sweeping
+ * the background, else 0. */
+int born_checkpoints_reused(const born_handle *h);
 
 /* Phase timing of born_lin_adjoint (off by default): with enable != 0 the
  * loop records a CUDA event at every phase boundary on the handle's stream

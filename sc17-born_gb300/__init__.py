@@ -95,6 +95,8 @@ _SIGS = {
     "born_autotune": (C.c_int, [_vp, C.c_int]),
     "born_tuned_config": (C.c_int, [_vp, C.c_int, _ip, _fp]),
     "born_loop_tile_ms": (C.c_int, [_vp, C.c_int, _fp, C.c_int]),
+    "born_set_checkpoint_interval": (C.c_int, [_vp, C.c_int]),
+    "born_checkpoints_reused": (C.c_int, [_vp]),
     "born_time_phases": (C.c_int, [_vp, C.c_int]),
     "born_phase_times": (C.c_int, [_vp, _fp, C.c_int]),
     "born_selftest_wait_timeout": (C.c_int, [_vp]),

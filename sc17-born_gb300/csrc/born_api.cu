@@ -791,6 +791,7 @@ int born_create_space(born_handle *h, float d1, float d2, float d3, float bc_a,
   CK(h, cudaStreamSynchronize(h->stream));
   h->have_space = true;
   h->generation++;
+  h->bg_gen++;
   h->reset_tuning();  // tile choices are per grid
   return BORN_OK;
 }
@@ -805,6 +806,7 @@ int born_set_sinc_table(born_handle *h, int which, int nsinc, int jt,
   if (which == 0) {
     h->tab_s = t;
     h->jt_s = jt;
+    h->bg_gen++;
   } else {
     h->tab_d = t;
     h->jt_d = jt;
@@ -817,6 +819,7 @@ int born_set_source_func(born_handle *h, int npts, int nt_big, const int *locs,
   int rc = check_ready(h);
   if (rc) return rc;
   h->src_levels_valid = false;
+  h->bg_gen++;
   return upload_points(h, h->src, npts, nt_big, locs, vals);
 }
 
@@ -840,6 +843,7 @@ int born_set_velocity(born_handle *h, int slot, int nx, int ny, int nz,
                         h->stream));
   CK(h, cudaStreamSynchronize(h->stream));
   (slot == 1 ? h->have_vel1 : h->have_vel2) = true;
+  if (slot == 2) h->bg_gen++;
   return BORN_OK;
 }
 
@@ -1161,50 +1165,6 @@ int born_model(born_handle *h, int jt, int nt, float *traces_out) {
   return BORN_OK;
 }
 
-int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
-  int rc = check_ready(h);
-  if (rc) return rc;
-  if (h->lp())
-    return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
-  if (nt < 0 || jt < 1) return fail(h, BORN_EINVAL, "nt < 0 or jt < 1");
-  if (!h->have_vel2 || !h->have_refl)
-    return fail(h, BORN_ESTATE, "vel2 or model perturbation not transferred");
-  if (jt > h->jt_s || jt > h->jt_d)
-    return fail(h, BORN_EINVAL, "jt %d exceeds the sinc tables' rows", jt);
-  rc = ensure_tuned(h, born::kModeBornLin);
-  if (rc) return rc;
-  const size_t bytes = (size_t)h->n123 * 4;
-  CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
-  CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
-  CK(h, cudaMemsetAsync(h->r0, 0, bytes, h->stream));
-  CK(h, cudaMemsetAsync(h->r1, 0, bytes, h->stream));
-  float *sp0 = h->f0, *sp1 = h->f1, *rp0 = h->r0, *rp1 = h->r1;
-  const float scale = 1 / (float)jt;
-  for (int it = 0; it < nt; ++it) {
-    const int id = it / jt, ii = it - id * jt;
-    StepParams p;
-    base_params(h, p);
-    p.a_out = sp0;
-    p.b_out = rp0;
-    p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
-    p.pb = point_view(h->rec, id, ii, h->tab_d, 0.f, true);
-    const void *cen[born::kNumCentre] = {sp0, rp0, h->vel2, nullptr,
-                                          h->refl};
-    rc = launch(h, born::kModeBornLin, true, true, sp1, rp1, cen, p);
-    if (!rc) rc = poll_error(h, it);
-    if (rc) return rc;
-    std::swap(sp0, sp1);
-    std::swap(rp0, rp1);
-  }
-  if (traces_out) {
-    CK(h, cudaMemcpyAsync(traces_out, h->rec.traces,
-                          (size_t)h->rec.npts * h->rec.nt * 4,
-                          cudaMemcpyDeviceToHost, h->stream));
-    return check_device_error(h);
-  }
-  return BORN_OK;
-}
-
 namespace {
 // CUDA events recorded one after another on the handle's stream (none when
 // count is 0); elapsed() waits for the later event.
@@ -1247,6 +1207,74 @@ int ensure_levels(born_handle *h, float **buf, size_t *have, size_t levels) {
 }
 }  // namespace
 
+int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
+  int rc = check_ready(h);
+  if (rc) return rc;
+  if (h->lp())
+    return fail(h, BORN_ESTATE, "%s needs FP32 storage", __func__);
+  if (nt < 0 || jt < 1) return fail(h, BORN_EINVAL, "nt < 0 or jt < 1");
+  if (!h->have_vel2 || !h->have_refl)
+    return fail(h, BORN_ESTATE, "vel2 or model perturbation not transferred");
+  if (jt > h->jt_s || jt > h->jt_d)
+    return fail(h, BORN_EINVAL, "jt %d exceeds the sinc tables' rows", jt);
+  rc = ensure_tuned(h, born::kModeBornLin);
+  if (rc) return rc;
+  const size_t n = (size_t)h->n123, bytes = n * 4;
+  // the background computed here is the one born_lin_adjoint checkpoints:
+  // store its checkpoints on the way (two levels every ckpt_every steps)
+  const int every = h->ckpt_every;
+  h->ckpt_valid = false;
+  if (every > 0) {
+    rc = ensure_levels(h, &h->ckpt, &h->ckpt_levels,
+                       2 * (size_t)((nt + every - 1) / every));
+    if (rc) return rc;
+  }
+  CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->r0, 0, bytes, h->stream));
+  CK(h, cudaMemsetAsync(h->r1, 0, bytes, h->stream));
+  float *sp0 = h->f0, *sp1 = h->f1, *rp0 = h->r0, *rp1 = h->r1;
+  const float scale = 1 / (float)jt;
+  for (int it = 0; it < nt; ++it) {
+    if (every > 0 && it % every == 0) {
+      float *ck = h->ckpt + 2 * (size_t)(it / every) * n;
+      CK(h, cudaMemcpyAsync(ck, sp0, bytes, cudaMemcpyDeviceToDevice,
+                            h->stream));
+      CK(h, cudaMemcpyAsync(ck + n, sp1, bytes, cudaMemcpyDeviceToDevice,
+                            h->stream));
+    }
+    const int id = it / jt, ii = it - id * jt;
+    StepParams p;
+    base_params(h, p);
+    p.a_out = sp0;
+    p.b_out = rp0;
+    p.pa = point_view(h->src, id, ii, h->tab_s, scale, true);
+    p.pb = point_view(h->rec, id, ii, h->tab_d, 0.f, true);
+    const void *cen[born::kNumCentre] = {sp0, rp0, h->vel2, nullptr,
+                                          h->refl};
+    rc = launch(h, born::kModeBornLin, true, true, sp1, rp1, cen, p);
+    if (!rc) rc = poll_error(h, it);
+    if (rc) return rc;
+    std::swap(sp0, sp1);
+    std::swap(rp0, rp1);
+  }
+  if (every > 0) {
+    h->ckpt_valid = true;
+    h->ckpt_gen = h->bg_gen;
+    h->ckpt_jt = jt;
+    h->ckpt_nt = nt;
+    h->ckpt_interval = every;
+  }
+  if (traces_out) {
+    CK(h, cudaMemcpyAsync(traces_out, h->rec.traces,
+                          (size_t)h->rec.npts * h->rec.nt * 4,
+                          cudaMemcpyDeviceToHost, h->stream));
+    return check_device_error(h);
+  }
+  return BORN_OK;
+}
+
+
 int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
                      float *model_out) {
   int rc = check_ready(h);
@@ -1283,21 +1311,36 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
                                           nullptr};
     return launch(h, born::kModeModel, true, false, sp1, nullptr, cen, p);
   };
-  // forward sweep of the background, checkpointing (old, cur) per segment
-  CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
-  CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
-  float *sp0 = h->f0, *sp1 = h->f1;
-  for (int it = 0; it < nt; ++it) {
-    if (it % interval == 0) {
-      float *ck = h->ckpt + 2 * (size_t)(it / interval) * n;
-      CK(h, cudaMemcpyAsync(ck, sp0, bytes, cudaMemcpyDeviceToDevice, h->stream));
-      CK(h, cudaMemcpyAsync(ck + n, sp1, bytes, cudaMemcpyDeviceToDevice,
-                            h->stream));
+  // forward sweep of the background, checkpointing (old, cur) per segment,
+  // unless the checkpoints of this background are already there (left by
+  // born_lin_forward or an earlier adjoint)
+  const bool have_ckpt = h->ckpt_valid && h->ckpt_gen == h->bg_gen &&
+                         h->ckpt_jt == jt && h->ckpt_nt == nt &&
+                         h->ckpt_interval == interval;
+  h->ckpt_reused = have_ckpt;
+  if (!have_ckpt) {
+    h->ckpt_valid = false;
+    CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
+    CK(h, cudaMemsetAsync(h->f1, 0, bytes, h->stream));
+    float *sp0 = h->f0, *sp1 = h->f1;
+    for (int it = 0; it < nt; ++it) {
+      if (it % interval == 0) {
+        float *ck = h->ckpt + 2 * (size_t)(it / interval) * n;
+        CK(h, cudaMemcpyAsync(ck, sp0, bytes, cudaMemcpyDeviceToDevice,
+                              h->stream));
+        CK(h, cudaMemcpyAsync(ck + n, sp1, bytes, cudaMemcpyDeviceToDevice,
+                              h->stream));
+      }
+      rc = model_step(sp0, sp1, it, nullptr);
+      if (!rc) rc = poll_error(h, it);
+      if (rc) return rc;
+      std::swap(sp0, sp1);
     }
-    rc = model_step(sp0, sp1, it, nullptr);
-    if (!rc) rc = poll_error(h, it);
-    if (rc) return rc;
-    std::swap(sp0, sp1);
+    h->ckpt_valid = true;
+    h->ckpt_gen = h->bg_gen;
+    h->ckpt_jt = jt;
+    h->ckpt_nt = nt;
+    h->ckpt_interval = interval;
   }
   rc = pe.record();
   if (rc) return rc;
@@ -1476,6 +1519,17 @@ int born_loop_tile_ms(const born_handle *h, int mode, float *ms, int n) {
     ms[c] = c < born_handle::kMaxTileCfgs ? h->loop_ms[h->storage][mode][c]
                                           : 0.f;
   return BORN_OK;
+}
+
+int born_set_checkpoint_interval(born_handle *h, int interval) {
+  if (!h) return BORN_EINVAL;
+  if (interval < 0) return fail(h, BORN_EINVAL, "checkpoint interval < 0");
+  h->ckpt_every = interval;
+  return BORN_OK;
+}
+
+int born_checkpoints_reused(const born_handle *h) {
+  return h ? (h->ckpt_reused ? 1 : 0) : BORN_EINVAL;
 }
 
 int born_time_phases(born_handle *h, int enable) {

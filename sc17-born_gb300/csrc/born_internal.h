@@ -136,6 +136,17 @@ struct born_handle {
   // exact linearised adjoint: checkpoints and the per-segment A s buffer
   float *ckpt = nullptr, *gbuf = nullptr;
   size_t ckpt_levels = 0, gbuf_levels = 0;
+  // The background s of the exact pair depends only on vel2, the source
+  // (points, traces, source sinc table) and the grid: bg_gen counts changes
+  // of those, and the checkpoints in ckpt are reusable while (bg_gen, jt,
+  // nt, interval) equal ckpt_key.  born_lin_forward stores them every
+  // ckpt_every steps (0: never) as it computes the background.
+  unsigned long long bg_gen = 1;
+  bool ckpt_valid = false;
+  unsigned long long ckpt_gen = 0;
+  int ckpt_jt = 0, ckpt_nt = 0, ckpt_interval = 0;
+  int ckpt_every = 50;
+  bool ckpt_reused = false;  // the last born_lin_adjoint skipped its sweep
   // phase times (ms) of the last born_lin_adjoint when timing is enabled:
   // forward sweep with checkpoint stores, segment restores and recompute,
   // reverse adjoint steps, final division (born_phase_times)

@@ -149,6 +149,7 @@ extern "C" int born_make_velocity(born_handle *h, int slot, const float *vel,
     return born_fail(h, BORN_ECUDA, "born_make_velocity: %s",
                      cudaGetErrorString(e));
   (slot == 1 ? h->have_vel1 : h->have_vel2) = true;
+  if (slot == 2) h->bg_gen++;
   return BORN_OK;
 }
 

@@ -168,3 +168,43 @@ def test_lin_adjoint_phase_timing(gpu, po):
     assert np.array_equal(got, want)
     assert all(v > 0 for v in ms), ms
     assert sum(ms) <= wall_ms, (ms, wall_ms)
+
+
+def test_lin_adjoint_reuses_forward_checkpoints(gpu, po):
+    """born_lin_forward stores the background's checkpoints as it computes
+    the background; born_lin_adjoint then skips its own checkpointing sweep
+    (born_checkpoints_reused) and gives the same gradient bit for bit as
+    with the sweep.  Any change of vel2 or the source makes it sweep again."""
+    c = case(po, seed=84, nt=110)
+    g = gpu.Gb300Prop()
+    setup(g, c)
+    L = g.lib
+    rng = np.random.default_rng(6)
+    m = (1e-3 * rng.standard_normal(c["shape"])).astype(np.float32)
+    tr = rng.standard_normal(c["rec_in"].shape).astype(np.float32)
+    # without stored checkpoints: the adjoint sweeps
+    g.check(L.born_set_checkpoint_interval(g.h, 0))
+    d0 = g.lin_forward(c["jts"], c["nt"], m)
+    want = g.lin_adjoint(c["jts"], c["nt"], tr, interval=20)
+    assert L.born_checkpoints_reused(g.h) == 0
+    # the adjoint's own checkpoints serve the next adjoint
+    again = g.lin_adjoint(c["jts"], c["nt"], tr, interval=20)
+    assert L.born_checkpoints_reused(g.h) == 1
+    assert np.array_equal(again, want)
+    # checkpoints stored by the forward
+    g.check(L.born_set_checkpoint_interval(g.h, 20))
+    d1 = g.lin_forward(c["jts"], c["nt"], m)
+    assert np.array_equal(d0, d1)
+    got = g.lin_adjoint(c["jts"], c["nt"], tr, interval=20)
+    assert L.born_checkpoints_reused(g.h) == 1
+    assert np.array_equal(got, want)
+    # another interval, or a changed vel2: a fresh sweep, same gradient
+    g.lin_forward(c["jts"], c["nt"], m)
+    other = g.lin_adjoint(c["jts"], c["nt"], tr, interval=15)
+    assert L.born_checkpoints_reused(g.h) == 0
+    assert np.array_equal(other, want)
+    nz, ny, nx = c["shape"]
+    g.lin_forward(c["jts"], c["nt"], m)
+    g.transferVelFunc2(nx, ny, nz, c["vel2"] * np.float32(1.01))
+    g.lin_adjoint(c["jts"], c["nt"], tr, interval=20)
+    assert L.born_checkpoints_reused(g.h) == 0
