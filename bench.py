@@ -871,30 +871,14 @@ def run_lsrtm(args):
     import torch
     born = package()
     born.lib()
-    n1 = n2 = args.model_n or 128     # the full config: 384 x 384 x 256
-    n3 = max(32, (2 * n1) // 3)
-    d, nt_data, dt_data, f = 10.0, args.nt or 400, 0.001, 15.0
-    rng = np.random.default_rng(1005)
-    z = np.arange(n3, dtype=np.float32)[:, None, None]
-    x = np.arange(n1, dtype=np.float32)[None, None, :]
-    vel = 1500.0 + 2500.0 * z / (n3 - 1) + 0 * x
-    vel = np.where(z > 0.5 * n3 + 0.1 * (x - n1 / 2), vel + 300.0, vel)
-    vel = np.broadcast_to(vel, (n3, n2, n1)).astype(np.float32)
-    m_true = np.zeros((n3, n2, n1), np.float32)
-    for zl in rng.choice(np.arange(n3 // 4, n3 - 8), size=6, replace=False):
-        m_true[zl] = rng.choice([-1.0, 1.0]) * 1e-3  # sparse layered spikes
-    ns = int(round(np.sqrt(args.shots)))
-    sx = (np.arange(ns) + 0.5) * (n1 * d / ns)
-    shots = np.array([[a, b, 2 * d] for b in sx for a in sx], np.float32)
-    t = -1.2 / f + np.arange(nt_data) * dt_data
-    a = (np.pi * f * t) ** 2
-    wav = ((1 - 2 * a) * np.exp(-a)).astype(np.float32)
-    nr = max(8, n1 // 2)
+    wl = workload_module()
+    kw, m_true = wl.c5_problem(model_n=args.model_n or 128,
+                               nshots=args.shots, nt_data=args.nt or 400)
+    n3, n2, n1 = m_true.shape
+    d, nt_data = kw["d"][0], kw["nt_data"]
+    shots = kw["shots"]
     t0 = time.perf_counter()
-    rd = d * (n1 - 2) / nr  # receivers spread over the model surface
-    op = born.BornOperator(vel, (0., 0., 0.), (d, d, d), shots, wav, dt_data,
-                           nt_data, dt_data, (nr, nr), (d, d), (rd, rd), d,
-                           40, exact=True, ckpt_interval=50)
+    op = born.BornOperator(exact=True, ckpt_interval=50, **kw)
     setup_s = time.perf_counter() - t0
     mt = torch.from_numpy(m_true).cuda()
     d_obs = torch.zeros(op.data_shape, device="cuda")

@@ -100,6 +100,11 @@ void oracle_lin_forwardf(oracle_propf *s, int jt, const float *m, float *rec,
 void oracle_modeld(oracle_propd *s, int jt, double *rec, int nt);
 void oracle_lin_forwardd(oracle_propd *s, int jt, const double *m,
                          double *rec, int nt);
+/* exact adjoint of oracle_lin_forward: mbar (n123) from traces rec */
+void oracle_lin_adjointf(oracle_propf *s, int jt, const float *rec,
+                         float *mbar, int nt);
+void oracle_lin_adjointd(oracle_propd *s, int jt, const double *rec,
+                         double *mbar, int nt);
 
 /* ---- double (accuracy) oracle ---- */
 void oracle_source_propd(oracle_propd *s, double *p0, double *p1, int jts,

@@ -312,6 +312,85 @@ void FN(oracle_lin_forward)(PROPT *s, int jt, const REAL *m, REAL *rec,
   free(g);
 }
 
+/* Exact adjoint of oracle_lin_forward (no reference counterpart: the
+ * reference's RTM adjoint is not the transpose of its Born forward).  The
+ * forward is the state recursion, per step t (taper B, stencil A, V = vel2,
+ * g_t = A s_t the background's stencil sum, E_t the trace extraction):
+ *   x_{t+1} = B y_t,   y_{t+1} = B (V A y_t + 2 y_t - x_t + m g_t),
+ *   d_t = E_t y_{t+1},   x_0 = y_0 = 0,
+ * whose transpose in z_t = B ybar_{t+1} is, for t = nt-1 .. 0,
+ *   z_t = B (A (V z_{t+1}) + 2 z_{t+1} - B z_{t+2} + E_t^T d_t),
+ *   mbar = sum_t g_t z_t
+ * (A restricted to the interior is symmetric; the exterior band is never
+ * written).  All g_t are kept (n123 x nt values: small grids only).  rec:
+ * the traces d [nrec][nt_rec]; mbar (n123) is overwritten. */
+void FN(oracle_lin_adjoint)(PROPT *s, int jt, const REAL *rec, REAL *mbar,
+                            int nt) {
+  s->jt = jt;
+  s->dir = 1;
+  const size_t n = (size_t)s->n123;
+  REAL *g = (REAL *)calloc(n * (size_t)(nt > 0 ? nt : 1), sizeof(REAL));
+  REAL *b0 = (REAL *)calloc(n, sizeof(REAL)), *b1 = (REAL *)calloc(n, sizeof(REAL));
+  REAL *s_p0 = b0, *s_p1 = b1;
+  for (int it = 0; it < nt; it++) {
+    int id = it / jt, ii = it - id * jt;
+    FN(oracle_stencil_sum)(s, s_p1, g + n * (size_t)it);
+    FN(oracle_prop_step)(s, s_p0, s_p1, s->vel2);
+    FN(oracle_damp)(s, s_p0, s_p1);
+    FN(oracle_inject_source)(s, id, ii, s_p0);
+    REAL *pt = s_p0;
+    s_p0 = s_p1;
+    s_p1 = pt;
+  }
+  REAL *z0 = (REAL *)calloc(n, sizeof(REAL)), *z1 = (REAL *)calloc(n, sizeof(REAL));
+  REAL *z2 = (REAL *)calloc(n, sizeof(REAL)), *vz = (REAL *)calloc(n, sizeof(REAL));
+  REAL *a = (REAL *)calloc(n, sizeof(REAL)), *one = (REAL *)malloc(n * sizeof(REAL));
+  for (size_t i = 0; i < n; i++) {
+    mbar[i] = 0;
+    one[i] = 1;
+  }
+  /* the taper factor of every cell: oracle_damp applied to ones */
+  REAL *bt = (REAL *)malloc(n * sizeof(REAL));
+  for (size_t i = 0; i < n; i++) bt[i] = 1;
+  FN(oracle_damp)(s, bt, one);
+  for (int it = nt - 1; it >= 0; it--) {
+    int id = it / jt, ii = it - id * jt;
+    for (size_t i = 0; i < n; i++) vz[i] = s->vel2[i] * z1[i];
+    FN(oracle_stencil_sum)(s, vz, a);
+    for (size_t i = 0; i < n; i++)
+      z0[i] = a[i] + 2 * z1[i] - bt[i] * z2[i];
+    /* E_t^T d_t: the transpose of oracle_data_extract */
+    if (id + 7 < s->nt_rec) {
+      const REAL *t = s->table_d + (long long)ii * s->nsinc_d;
+      for (int r = 0; r < s->nrec; r++) {
+        const REAL *v = rec + (long long)s->nt_rec * r + id;
+        REAL acc = 0;
+        for (int k = 0; k < 8; k++) acc += t[k] * v[k];
+        z0[s->locs_r[r]] += acc;
+      }
+    }
+    const REAL *gt = g + n * (size_t)it;
+    for (size_t i = 0; i < n; i++) {
+      z0[i] *= bt[i];
+      mbar[i] += gt[i] * z0[i];
+    }
+    REAL *pt = z2;
+    z2 = z1;
+    z1 = z0;
+    z0 = pt;
+  }
+  free(g);
+  free(b0);
+  free(b1);
+  free(z0);
+  free(z1);
+  free(z2);
+  free(vz);
+  free(a);
+  free(one);
+  free(bt);
+}
+
 #undef FN
 #undef PROPT
 #undef CAT

@@ -184,6 +184,8 @@ def port_lib():
             "oracle_lin_forwardf": (None, [P, C.c_int, _fp, _fp, C.c_int]),
             "oracle_modeld": (None, [PD, C.c_int, _dp, C.c_int]),
             "oracle_lin_forwardd": (None, [PD, C.c_int, _dp, _dp, C.c_int]),
+            "oracle_lin_adjointf": (None, [P, C.c_int, _fp, _fp, C.c_int]),
+            "oracle_lin_adjointd": (None, [PD, C.c_int, _dp, _dp, C.c_int]),
             "oracle_sinc_table": (None, [C.c_int, C.c_int, _fp]),
             "oracle_calc_stability": (C.c_float, [C.c_float, C.c_float,
                                                   C.c_float, C.c_int, _ip]),
@@ -355,6 +357,15 @@ class PortProp:
         self.lib.oracle_lin_forwardf(C.byref(self.s), jt, fptr(m), fptr(rec),
                                      nt)
 
+    def lin_adjoint(self, jt, rec, nt):
+        """Exact adjoint of lin_forward applied to the traces rec
+        ([nrec][nt_rec]); returns the model-space result (n123)."""
+        rec = self._arr(rec)
+        out = np.zeros(self.shape, self.dtype)
+        self.lib.oracle_lin_adjointf(C.byref(self.s), jt, fptr(rec),
+                                     fptr(out), nt)
+        return out
+
     # primitives, for unit tests
     def prop(self, p0, p1, vel):
         self.lib.oracle_prop_stepf(C.byref(self.s), fptr(p0), fptr(p1),
@@ -406,6 +417,13 @@ class PortProp64(PortProp):
         self._keep["rec"] = rec
         self.lib.oracle_lin_forwardd(C.byref(self.s), jt, dptr(m), dptr(rec),
                                      nt)
+
+    def lin_adjoint(self, jt, rec, nt):
+        rec = self._arr(rec)
+        out = np.zeros(self.shape, self.dtype)
+        self.lib.oracle_lin_adjointd(C.byref(self.s), jt, dptr(rec),
+                                     dptr(out), nt)
+        return out
 
 
 class RefProp:

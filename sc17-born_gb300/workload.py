@@ -248,3 +248,40 @@ def prepare_batch_c4(born, nshots=48, nt=2500, nbound=40, f=15.0,
         h.transferReceiverFunc(nrx, nry, nt_big, locs_r, rec)
         handles.append(h)
     return handles, dict(nt=nt_fd, jt=jt, nbound=nbound)
+
+
+# ---------------------------------------------------------------------------
+# c5: least-squares RTM by CG over several shots
+
+def c5_problem(model_n=128, nshots=16, nt_data=400, nbound=40, d=10.0,
+               f=15.0, dt_data=0.001, seed=1005):
+    """The c5 inversion problem: model_n x model_n x max(32, 2 model_n / 3)
+    cells at d, layered 1500..4000 m/s with a dipping +300 m/s step,
+    sqrt(nshots) x sqrt(nshots) sources 2 d deep, receivers over the model
+    surface, a Ricker wavelet, and the true reflectivity: six seeded
+    z-planes of +-1e-3.  Returns (keyword arguments of BornOperator,
+    m_true)."""
+    n1 = n2 = model_n
+    n3 = max(32, (2 * n1) // 3)
+    rng = np.random.default_rng(seed)
+    z = np.arange(n3, dtype=np.float32)[:, None, None]
+    x = np.arange(n1, dtype=np.float32)[None, None, :]
+    vel = 1500.0 + 2500.0 * z / (n3 - 1) + 0 * x
+    vel = np.where(z > 0.5 * n3 + 0.1 * (x - n1 / 2), vel + 300.0, vel)
+    vel = np.broadcast_to(vel, (n3, n2, n1)).astype(np.float32)
+    m_true = np.zeros((n3, n2, n1), np.float32)
+    for zl in rng.choice(np.arange(n3 // 4, n3 - 8), size=6, replace=False):
+        m_true[zl] = rng.choice([-1.0, 1.0]) * 1e-3
+    ns = int(round(np.sqrt(nshots)))
+    sx = (np.arange(ns) + 0.5) * (n1 * d / ns)
+    shots = np.array([[a, b, 2 * d] for b in sx for a in sx], np.float32)
+    t = -1.2 / f + np.arange(nt_data) * dt_data
+    a = (np.pi * f * t) ** 2
+    wav = ((1 - 2 * a) * np.exp(-a)).astype(np.float32)
+    nr = max(8, n1 // 2)
+    rd = d * (n1 - 2) / nr  # receivers spread over the model surface
+    kw = dict(velocity=vel, o=(0., 0., 0.), d=(d, d, d), shots=shots,
+              wavelet=wav, dt_wavelet=dt_data, nt_data=nt_data,
+              dt_data=dt_data, rec_n=(nr, nr), rec_o=(d, d), rec_d=(rd, rd),
+              rec_depth=d, nbound=nbound)
+    return kw, m_true

@@ -1,0 +1,137 @@
+"""The exact linearised pair and least-squares RTM against FP64 oracles.
+
+* born_lin_adjoint against oracle_lin_adjoint (the exact transpose of the
+  oracle's linearised forward, restated in C): the GPU forms the adjoint in
+  the variable w = v^2 dt^2 z and divides by v^2 dt^2 at the end, the
+  oracle works in z, so the two agree to FP32 rounding, not bit for bit;
+  they are compared with the FP32 oracle's own distance from the FP64 one
+  as the yardstick.
+* the exact Born operator (born_op, exact = 1) forward and adjoint against
+  the FP64 restatement of the whole chain (tests/exact_op64.py);
+* born_cg_solve (FP32 operator, FP64 dots and step lengths) against
+  Claerbout's CG in FP64 on the FP64 operator, on a reduced c5 problem
+  (4 shots, 40 x 40 x 32 model, 200 samples): rr.rr after every iteration
+  and the model after the last.  Both decrease rr.rr as slowly (about 15 %
+  in 10 iterations): the slow convergence of unpreconditioned least-squares
+  migration here is the problem's, not the FP32 arithmetic's.
+"""
+import importlib.util
+import os
+
+import numpy as np
+import pytest
+
+import cases
+from exact_op64 import ExactOperator64, cgstep_solve
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm((a - b).ravel()) /
+                 max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+def workload():
+    spec = importlib.util.spec_from_file_location(
+        "born_gb300_workload",
+        os.path.join(ROOT, "sc17-born_gb300", "workload.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.fixture(scope="module")
+def torch_cuda(born):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    return torch
+
+
+@pytest.mark.parametrize("jt", [1, 2])
+def test_lin_adjoint_matches_oracle(born, po, torch_cuda, jt):
+    c = cases.make_case(91 + jt, shape=(36, 40, 48), nt=100, jt=jt,
+                        sinc=po.sinc_table)
+    rng = np.random.default_rng(17)
+    tr = rng.standard_normal(c["rec_in"].shape).astype(np.float32)
+    g = born.Gb300Prop()
+    nz, ny, nx = c["shape"]
+    g.createSpace(c["d"], c["d"], c["d"], 50, .0005, .0005, nx, ny, nz)
+    g.transferSincTableS(8, c["jts"], c["table_s"])
+    g.transferSincTableD(8, c["jtd"], c["table_d"])
+    g.transferSourceFunc(9, c["nt_big"], c["locs_s"], c["src"])
+    g.transferVelFunc1(nx, ny, nz, c["vel1"])
+    g.transferVelFunc2(nx, ny, nz, c["vel2"])
+    g.transferReceiverFunc(c["rec_nx"], c["rec_ny"], c["nt_big"],
+                           c["locs_r"], np.zeros_like(c["rec_in"]))
+    got = g.lin_adjoint(c["jts"], c["nt"], tr, interval=17)
+    outs = {}
+    for P in (po.PortProp, po.PortProp64):
+        o = P()
+        po.run_case(o, c, which="none")
+        rec = np.zeros(c["rec_in"].shape, o.dtype)
+        o.transferReceiverFunc(c["rec_nx"], c["rec_ny"], c["nt_big"],
+                               c["locs_r"], rec)
+        outs[P.__name__] = o.lin_adjoint(c["jts"], tr, c["nt"])
+    want64, want32 = outs["PortProp64"], outs["PortProp"]
+    assert np.linalg.norm(want64) > 0
+    e_gpu, e_32 = rel(got, want64), rel(want32, want64)
+    print(f"jt={jt}: GPU vs FP64 {e_gpu:.3e}, FP32 oracle vs FP64 {e_32:.3e}")
+    assert e_gpu <= max(10 * e_32, 1e-5), (e_gpu, e_32)
+
+
+def test_exact_operator_matches_fp64_chain(born, po, torch_cuda):
+    torch = torch_cuda
+    from test_operator import setup_problem
+    kw = setup_problem(seed=9, nshots=2, nt_data=50)
+    op = born.BornOperator(exact=True, ckpt_interval=16, **kw)
+    op64 = ExactOperator64(po, kw)
+    assert op64.data_shape == op.data_shape and op64.nt == op.nt_fd
+    rng = np.random.default_rng(23)
+    m = rng.standard_normal(op.model_shape).astype(np.float32)
+    d = rng.standard_normal(op.data_shape).astype(np.float32)
+    lm = torch.zeros(op.data_shape, device="cuda")
+    op.forward(False, torch.from_numpy(m).cuda(), lm)
+    ltd = torch.zeros(op.model_shape, device="cuda")
+    op.adjoint(False, ltd, torch.from_numpy(d).cuda())
+    e_f = rel(lm.cpu().numpy(), op64.forward(m))
+    e_a = rel(ltd.cpu().numpy(), op64.adjoint(d))
+    print(f"operator vs FP64: forward {e_f:.3e}, adjoint {e_a:.3e}")
+    assert e_f <= 1e-5 and e_a <= 1e-5, (e_f, e_a)
+
+
+def test_cg_matches_fp64_cg(born, po, torch_cuda):
+    torch = torch_cuda
+    po.set_threads(os.cpu_count() or 1)
+    kw, m_true = workload().c5_problem(model_n=40, nshots=4, nt_data=200,
+                                       nbound=10)
+    op = born.BornOperator(exact=True, ckpt_interval=50, **kw)
+    op64 = ExactOperator64(po, kw)
+    niter = 10
+    d_obs = torch.zeros(op.data_shape, device="cuda")
+    op.forward(False, torch.from_numpy(m_true).cuda(), d_obs)
+    m = torch.zeros(op.model_shape, device="cuda")
+    res = op.cg(d_obs, m, niter)
+    m64, res64 = cgstep_solve(op64.forward, op64.adjoint,
+                              op64.forward(m_true), niter)
+    r, r64 = np.array(res), np.array(res64)
+    print("rr/rr0 GPU ", np.round(r / r[0], 5).tolist())
+    print("rr/rr0 FP64", np.round(r64 / r64[0], 5).tolist())
+    e_r = np.abs(r / r64 - 1)
+    e_m = rel(m.cpu().numpy(), m64)
+    print(f"rr rel diff per iteration {np.round(e_r, 7).tolist()}, "
+          f"model vs FP64 solution {e_m:.3e}")
+    # identical to FP32 rounding of the operator (~1.5e-6) while the Krylov
+    # space is well conditioned; the last iterations reach directions of
+    # small singular values, where FP32 rounding of the operator is
+    # amplified (measured on GB300: 3.8e-5 and 1.1e-3 at iterations 9, 10;
+    # model 7.2e-3 from the FP64 solution)
+    assert np.all(e_r[:9] <= 1e-5), e_r
+    assert np.all(e_r <= 5e-3), e_r
+    assert e_m <= 2e-2, e_m
+    # both converge as slowly: unpreconditioned migration, not precision
+    assert 0.5 < r64[-1] / r64[0] < 1.0 and 0.5 < r[-1] / r[0] < 1.0
