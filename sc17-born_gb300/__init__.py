@@ -176,6 +176,11 @@ _SIGS = {
     "born_sep_read_info": (C.c_int, [C.c_char_p, _vp]),
     "born_sep_read": (C.c_int, [C.c_char_p, _fp, C.c_longlong]),
     "born_sep_write": (C.c_int, [C.c_char_p, _vp, _fp, C.c_int]),
+    "born_json_read_info": (C.c_int, [C.c_char_p, _vp]),
+    "born_regfile_read_info": (C.c_int, [C.c_char_p, _vp]),
+    "born_regfile_read": (C.c_int, [C.c_char_p, _fp, C.c_longlong]),
+    "born_regfile_write": (C.c_int, [C.c_char_p, _vp, _fp]),
+    "born_add_regfiles": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p]),
 }
 
 _lib = None
@@ -830,3 +835,34 @@ def write_sep(path: str, array, o=None, d=None, big_endian: bool = True):
         info.d[i] = 1.0 if d is None else d[i]
     _ck(lib().born_sep_write(path.encode(), C.byref(info), fptr(a),
                              int(big_endian)))
+
+
+def read_regfile(path: str):
+    """Reads a SEP or JSON regular file (by name: ".json" is JSON); returns
+    (array, o, d) with the axes reversed (n1 fastest)."""
+    info = SepInfo()
+    _ck(lib().born_regfile_read_info(path.encode(), C.byref(info)))
+    k = max(info.ndim, 1)
+    shape = tuple(int(info.n[a]) for a in range(k))
+    out = np.empty(int(np.prod(shape)), np.float32)
+    _ck(lib().born_regfile_read(path.encode(), fptr(out), out.size))
+    return out.reshape(shape[::-1]), tuple(info.o[:k]), tuple(info.d[:k])
+
+
+def write_regfile(path: str, array, o=None, d=None):
+    """Writes a SEP (big-endian data in path + '@') or, for names ending in
+    '.json', a JSON regular file (host-order data in path + '.dat')."""
+    a = f32(array)
+    shape = a.shape[::-1]
+    info = SepInfo()
+    info.ndim = len(shape)
+    for i, n in enumerate(shape):
+        info.n[i] = n
+        info.o[i] = 0.0 if o is None else o[i]
+        info.d[i] = 1.0 if d is None else d[i]
+    _ck(lib().born_regfile_write(path.encode(), C.byref(info), fptr(a)))
+
+
+def add_regfiles(in1: str, in2: str, out: str):
+    """util/Add: out = in1 + in2 (regular files of the same size)."""
+    _ck(lib().born_add_regfiles(in1.encode(), in2.encode(), out.encode()))

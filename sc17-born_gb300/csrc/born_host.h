@@ -105,6 +105,21 @@ int born_sep_read(const char *header, float *out, long long count);
 /* writes header and header@ (binary), big_endian selects xdr_float */
 int born_sep_write(const char *header, const born_sep_info *info,
                    const float *data, int big_endian);
+/* JSON regular files (the other kind SEP genericIO reads; the form
+ * scripts/run.py:20-36 writes): a JSON object with n1.., o1.., d1..,
+ * label1.. and "filename" (the data file, relative to the JSON's folder),
+ * 4-byte floats in host order unless "data_format" is "xdr_float". */
+int born_json_read_info(const char *path, born_sep_info *info);
+/* Either kind, by name: paths ending in ".json" are JSON, others SEP.
+ * Writing makes a SEP header with big-endian data in path + "@", or a JSON
+ * description with host-order data in path + ".dat". */
+int born_regfile_read_info(const char *path, born_sep_info *info);
+int born_regfile_read(const char *path, float *out, long long count);
+int born_regfile_write(const char *path, const born_sep_info *info,
+                       const float *data);
+/* util/Add (util/Add.cc:5-41): out = in1 + in2 (same sizes, else
+ * BORN_EINVAL); out takes in1's axes and may be in1 or in2. */
+int born_add_regfiles(const char *in1, const char *in2, const char *out);
 
 #ifdef __cplusplus
 }
