@@ -213,6 +213,14 @@ int born_set_checkpoint_interval(born_handle *h, int interval);
 /* 1 when the last born_lin_adjoint reused checkpoints instead of sweeping
  * the background, else 0. */
 int born_checkpoints_reused(const born_handle *h);
+/* Storage of the exact adjoint's checkpoints: FP32 (default; the gradient is
+ * the exact transpose), or FP16 with one power-of-two scale per checkpoint
+ * level, 2^(ceil(log2 max|level|) - 15), chosen on the device (half the
+ * memory; each segment is then recomputed from levels rounded to FP16, so
+ * the gradient is the transpose to about FP16 rounding). */
+#define BORN_CKPT_F32 0
+#define BORN_CKPT_F16 1
+int born_set_checkpoint_storage(born_handle *h, int storage);
 
 /* Phase timing of born_lin_adjoint (off by default): with enable != 0 the
  * loop records a CUDA event at every phase boundary on the handle's stream

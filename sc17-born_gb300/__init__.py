@@ -96,6 +96,7 @@ _SIGS = {
     "born_tuned_config": (C.c_int, [_vp, C.c_int, _ip, _fp]),
     "born_loop_tile_ms": (C.c_int, [_vp, C.c_int, _fp, C.c_int]),
     "born_set_checkpoint_interval": (C.c_int, [_vp, C.c_int]),
+    "born_set_checkpoint_storage": (C.c_int, [_vp, C.c_int]),
     "born_checkpoints_reused": (C.c_int, [_vp]),
     "born_time_phases": (C.c_int, [_vp, C.c_int]),
     "born_phase_times": (C.c_int, [_vp, _fp, C.c_int]),
@@ -463,6 +464,12 @@ class Gb300Prop(Handle):
         """born_lin_forward along the device reflectivity, traces left on
         the device (accumulated onto the current device traces)."""
         self.check(self.lib.born_lin_forward(self.h, jt, nt, None))
+
+    def set_checkpoint_storage(self, storage="f32"):
+        """Storage of the exact adjoint's checkpoints: "f32" or "f16" (one
+        power-of-two scale per level)."""
+        self.check(self.lib.born_set_checkpoint_storage(
+            self.h, {"f32": 0, "f16": 1}[storage]))
 
     def time_phases(self, enable=True):
         self.check(self.lib.born_time_phases(self.h, int(enable)))

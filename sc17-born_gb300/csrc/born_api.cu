@@ -84,8 +84,13 @@ void free_fields(born_handle *h) {
   }
   cudaFree(h->ckpt);
   cudaFree(h->gbuf);
+  cudaFree(h->ckpt_scale);
+  cudaFree(h->ckpt_maxw);
   h->ckpt = h->gbuf = nullptr;
-  h->ckpt_levels = h->gbuf_levels = 0;
+  h->ckpt_scale = nullptr;
+  h->ckpt_maxw = nullptr;
+  h->ckpt_levels = h->gbuf_levels = h->ckpt_bytes = h->ckpt_scale_levels = 0;
+  h->ckpt_valid = false;
   h->maps.clear();
   h->have_space = h->have_vel1 = h->have_vel2 = h->have_refl = false;
   h->src_levels_valid = false;
@@ -1205,6 +1210,66 @@ int ensure_levels(born_handle *h, float **buf, size_t *have, size_t levels) {
   *have = levels;
   return BORN_OK;
 }
+
+// Room for `levels` checkpoint levels in the handle's checkpoint storage
+// (FP32, or FP16 with one scale per level).  Reallocating drops the
+// checkpoints held.
+int ensure_ckpt(born_handle *h, size_t levels) {
+  const size_t esize = h->ckpt_storage == BORN_CKPT_F16 ? 2 : 4;
+  const size_t bytes = levels * (size_t)h->n123 * esize;
+  if (h->ckpt_bytes < bytes) {
+    cudaFree(h->ckpt);
+    h->ckpt = nullptr;
+    h->ckpt_bytes = 0;
+    h->ckpt_valid = false;
+    CK(h, cudaMalloc(&h->ckpt, bytes));
+    h->ckpt_bytes = bytes;
+  }
+  if (h->ckpt_storage == BORN_CKPT_F16) {
+    if (h->ckpt_scale_levels < levels) {
+      cudaFree(h->ckpt_scale);
+      h->ckpt_scale = nullptr;
+      h->ckpt_scale_levels = 0;
+      h->ckpt_valid = false;
+      CK(h, cudaMalloc(&h->ckpt_scale, levels * sizeof(float)));
+      h->ckpt_scale_levels = levels;
+    }
+    if (!h->ckpt_maxw) CK(h, cudaMalloc(&h->ckpt_maxw, sizeof(unsigned int)));
+  }
+  return BORN_OK;
+}
+
+// Checkpoint level k <- src (a copy, or an FP16 snapshot with its scale).
+int store_ckpt(born_handle *h, size_t k, const float *src) {
+  const size_t n = (size_t)h->n123;
+  if (h->ckpt_storage == BORN_CKPT_F16) {
+    unsigned short *base = reinterpret_cast<unsigned short *>(h->ckpt);
+    CK(h, born::launch_snapshot_f16(src, (long long)n, h->ckpt_maxw,
+                                    base + k * n, h->ckpt_scale + k,
+                                    h->stream));
+    h->launches += 2;
+    return BORN_OK;
+  }
+  CK(h, cudaMemcpyAsync(h->ckpt + k * n, src, n * 4, cudaMemcpyDeviceToDevice,
+                        h->stream));
+  return BORN_OK;
+}
+
+// dst <- checkpoint level k (FP32 values).
+int load_ckpt(born_handle *h, size_t k, float *dst) {
+  const size_t n = (size_t)h->n123;
+  if (h->ckpt_storage == BORN_CKPT_F16) {
+    const unsigned short *base =
+        reinterpret_cast<const unsigned short *>(h->ckpt);
+    CK(h, born::launch_restore_f16(base + k * n, (long long)n,
+                                   h->ckpt_scale + k, dst, h->stream));
+    h->launches++;
+    return BORN_OK;
+  }
+  CK(h, cudaMemcpyAsync(dst, h->ckpt + k * n, n * 4, cudaMemcpyDeviceToDevice,
+                        h->stream));
+  return BORN_OK;
+}
 }  // namespace
 
 int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
@@ -1225,8 +1290,7 @@ int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
   const int every = h->ckpt_every;
   h->ckpt_valid = false;
   if (every > 0) {
-    rc = ensure_levels(h, &h->ckpt, &h->ckpt_levels,
-                       2 * (size_t)((nt + every - 1) / every));
+    rc = ensure_ckpt(h, 2 * (size_t)((nt + every - 1) / every));
     if (rc) return rc;
   }
   CK(h, cudaMemsetAsync(h->f0, 0, bytes, h->stream));
@@ -1237,11 +1301,9 @@ int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
   const float scale = 1 / (float)jt;
   for (int it = 0; it < nt; ++it) {
     if (every > 0 && it % every == 0) {
-      float *ck = h->ckpt + 2 * (size_t)(it / every) * n;
-      CK(h, cudaMemcpyAsync(ck, sp0, bytes, cudaMemcpyDeviceToDevice,
-                            h->stream));
-      CK(h, cudaMemcpyAsync(ck + n, sp1, bytes, cudaMemcpyDeviceToDevice,
-                            h->stream));
+      rc = store_ckpt(h, 2 * (size_t)(it / every), sp0);
+      if (!rc) rc = store_ckpt(h, 2 * (size_t)(it / every) + 1, sp1);
+      if (rc) return rc;
     }
     const int id = it / jt, ii = it - id * jt;
     StepParams p;
@@ -1264,6 +1326,7 @@ int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
     h->ckpt_jt = jt;
     h->ckpt_nt = nt;
     h->ckpt_interval = every;
+    h->ckpt_kind = h->ckpt_storage;
   }
   if (traces_out) {
     CK(h, cudaMemcpyAsync(traces_out, h->rec.traces,
@@ -1291,7 +1354,7 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
   if (rc) return rc;
   const size_t n = (size_t)h->n123, bytes = n * 4;
   const int nseg = (nt + interval - 1) / interval;
-  rc = ensure_levels(h, &h->ckpt, &h->ckpt_levels, 2 * (size_t)nseg);
+  rc = ensure_ckpt(h, 2 * (size_t)nseg);
   if (!rc) rc = ensure_levels(h, &h->gbuf, &h->gbuf_levels, (size_t)interval);
   if (rc) return rc;
   const float scale = 1 / (float)jt;
@@ -1316,7 +1379,8 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
   // born_lin_forward or an earlier adjoint)
   const bool have_ckpt = h->ckpt_valid && h->ckpt_gen == h->bg_gen &&
                          h->ckpt_jt == jt && h->ckpt_nt == nt &&
-                         h->ckpt_interval == interval;
+                         h->ckpt_interval == interval &&
+                         h->ckpt_kind == h->ckpt_storage;
   h->ckpt_reused = have_ckpt;
   if (!have_ckpt) {
     h->ckpt_valid = false;
@@ -1325,11 +1389,9 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
     float *sp0 = h->f0, *sp1 = h->f1;
     for (int it = 0; it < nt; ++it) {
       if (it % interval == 0) {
-        float *ck = h->ckpt + 2 * (size_t)(it / interval) * n;
-        CK(h, cudaMemcpyAsync(ck, sp0, bytes, cudaMemcpyDeviceToDevice,
-                              h->stream));
-        CK(h, cudaMemcpyAsync(ck + n, sp1, bytes, cudaMemcpyDeviceToDevice,
-                              h->stream));
+        rc = store_ckpt(h, 2 * (size_t)(it / interval), sp0);
+        if (!rc) rc = store_ckpt(h, 2 * (size_t)(it / interval) + 1, sp1);
+        if (rc) return rc;
       }
       rc = model_step(sp0, sp1, it, nullptr);
       if (!rc) rc = poll_error(h, it);
@@ -1341,6 +1403,7 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
     h->ckpt_jt = jt;
     h->ckpt_nt = nt;
     h->ckpt_interval = interval;
+    h->ckpt_kind = h->ckpt_storage;
   }
   rc = pe.record();
   if (rc) return rc;
@@ -1352,11 +1415,10 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
   int steps = 0;
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int t0 = seg * interval, t1 = std::min(nt, t0 + interval);
-    const float *ck = h->ckpt + 2 * (size_t)seg * n;
     float *a0 = h->f0, *a1 = h->f1;
-    CK(h, cudaMemcpyAsync(a0, ck, bytes, cudaMemcpyDeviceToDevice, h->stream));
-    CK(h, cudaMemcpyAsync(a1, ck + n, bytes, cudaMemcpyDeviceToDevice,
-                          h->stream));
+    rc = load_ckpt(h, 2 * (size_t)seg, a0);
+    if (!rc) rc = load_ckpt(h, 2 * (size_t)seg + 1, a1);
+    if (rc) return rc;
     for (int it = t0; it < t1; ++it) {
       rc = model_step(a0, a1, it, h->gbuf + (size_t)(it - t0) * n);
       if (!rc) rc = poll_error(h, steps++);
@@ -1518,6 +1580,17 @@ int born_loop_tile_ms(const born_handle *h, int mode, float *ms, int n) {
   for (int c = 0; c < n; ++c)
     ms[c] = c < born_handle::kMaxTileCfgs ? h->loop_ms[h->storage][mode][c]
                                           : 0.f;
+  return BORN_OK;
+}
+
+int born_set_checkpoint_storage(born_handle *h, int storage) {
+  if (!h) return BORN_EINVAL;
+  if (storage != BORN_CKPT_F32 && storage != BORN_CKPT_F16)
+    return fail(h, BORN_EINVAL, "unknown checkpoint storage %d", storage);
+  if (storage != h->ckpt_storage) {
+    h->ckpt_storage = storage;
+    h->ckpt_valid = false;
+  }
   return BORN_OK;
 }
 

@@ -133,9 +133,16 @@ struct born_handle {
   // TMA descriptors by (buffer, tile config * 2 + kind); kind 0 = halo box,
   // 1 = centre tile
   std::map<std::pair<const void *, int>, CUtensorMap> maps;
-  // exact linearised adjoint: checkpoints and the per-segment A s buffer
+  // exact linearised adjoint: checkpoints (ckpt_bytes allocated; levels of
+  // n123 FP32 values, or FP16 values with one power-of-two scale per level
+  // in ckpt_scale) and the per-segment A s buffer
   float *ckpt = nullptr, *gbuf = nullptr;
   size_t ckpt_levels = 0, gbuf_levels = 0;
+  size_t ckpt_bytes = 0;
+  int ckpt_storage = 0;          // BORN_CKPT_F32 or BORN_CKPT_F16
+  float *ckpt_scale = nullptr;   // device, one scale per level (FP16)
+  size_t ckpt_scale_levels = 0;
+  unsigned int *ckpt_maxw = nullptr;  // device word for the level maxima
   // The background s of the exact pair depends only on vel2, the source
   // (points, traces, source sinc table) and the grid: bg_gen counts changes
   // of those, and the checkpoints in ckpt are reusable while (bg_gen, jt,
@@ -144,7 +151,7 @@ struct born_handle {
   unsigned long long bg_gen = 1;
   bool ckpt_valid = false;
   unsigned long long ckpt_gen = 0;
-  int ckpt_jt = 0, ckpt_nt = 0, ckpt_interval = 0;
+  int ckpt_jt = 0, ckpt_nt = 0, ckpt_interval = 0, ckpt_kind = 0;
   int ckpt_every = 50;
   bool ckpt_reused = false;  // the last born_lin_adjoint skipped its sweep
   // phase times (ms) of the last born_lin_adjoint when timing is enabled:

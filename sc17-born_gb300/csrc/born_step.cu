@@ -75,7 +75,53 @@ __global__ void absmax_kernel(const float *x, long long n, unsigned int *out) {
   if ((threadIdx.x & 31) == 0) atomicMax(out, w);
 }
 
+// FP16 snapshot of an FP32 level: the power-of-two scale
+// 2^(ceil(log2 max|x|) - 15) (pow2_scale_for, from the maximum the absmax
+// kernel left in *maxw) keeps every stored value within FP16's finite
+// range; each value is x / scale (an exact division) rounded to the nearest
+// FP16, and the scale is recorded in *scale_out.
+__global__ void snapshot_f16_kernel(const float *x, long long n,
+                                    const unsigned int *maxw, __half *out,
+                                    float *scale_out) {
+  const float scale = pow2_scale_for(__uint_as_float(*maxw));
+  const float inv = 1.f / scale;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    out[i] = __float2half_rn(clamp_f16(x[i] * inv));
+  if (blockIdx.x == 0 && threadIdx.x == 0) *scale_out = scale;
+}
+
+__global__ void restore_f16_kernel(const __half *in, long long n,
+                                   const float *scale, float *x) {
+  const float sc = *scale;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = __half2float(in[i]) * sc;
+}
+
 }  // namespace
+
+cudaError_t launch_snapshot_f16(const float *x, long long n,
+                                unsigned int *maxw, void *out, float *scale,
+                                cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(maxw, 0, sizeof(unsigned int), stream);
+  if (e != cudaSuccess) return e;
+  e = launch_absmax(x, n, maxw, stream);
+  if (e != cudaSuccess) return e;
+  const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+  snapshot_f16_kernel<<<blocks, 256, 0, stream>>>(
+      x, n, maxw, static_cast<__half *>(out), scale);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_restore_f16(const void *in, long long n,
+                               const float *scale, float *x,
+                               cudaStream_t stream) {
+  const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+  restore_f16_kernel<<<blocks, 256, 0, stream>>>(
+      static_cast<const __half *>(in), n, scale, x);
+  return cudaGetLastError();
+}
 
 unsigned centre_mask(int mode, bool pa, bool pb) {
   switch (mode) {

@@ -135,3 +135,48 @@ def test_cg_matches_fp64_cg(born, po, torch_cuda):
     assert e_m <= 2e-2, e_m
     # both converge as slowly: unpreconditioned migration, not precision
     assert 0.5 < r64[-1] / r64[0] < 1.0 and 0.5 < r[-1] / r[0] < 1.0
+
+
+def test_lin_adjoint_with_f16_checkpoints(born, po, torch_cuda):
+    """Checkpoints of the exact adjoint stored in FP16 with a power-of-two
+    scale per level (born_set_checkpoint_storage): each 50-step segment is
+    recomputed from levels rounded to FP16, so the gradient is no longer
+    the exact transpose, but it stays within 1e-3 of the FP64 oracle's,
+    which is the precision bar of 16-bit storage; FP16 checkpoints made by
+    the forward and by the adjoint's own sweep give the same gradient."""
+    c = cases.make_case(95, shape=(36, 40, 48), nt=200, jt=1,
+                        sinc=po.sinc_table)
+    rng = np.random.default_rng(19)
+    tr = rng.standard_normal(c["rec_in"].shape).astype(np.float32)
+    m = (1e-3 * rng.standard_normal(c["shape"])).astype(np.float32)
+    g = born.Gb300Prop()
+    nz, ny, nx = c["shape"]
+    g.createSpace(c["d"], c["d"], c["d"], 50, .0005, .0005, nx, ny, nz)
+    g.transferSincTableS(8, c["jts"], c["table_s"])
+    g.transferSincTableD(8, c["jtd"], c["table_d"])
+    g.transferSourceFunc(9, c["nt_big"], c["locs_s"], c["src"])
+    g.transferVelFunc1(nx, ny, nz, c["vel1"])
+    g.transferVelFunc2(nx, ny, nz, c["vel2"])
+    g.transferReceiverFunc(c["rec_nx"], c["rec_ny"], c["nt_big"],
+                           c["locs_r"], np.zeros_like(c["rec_in"]))
+    g32 = g.lin_adjoint(c["jts"], c["nt"], tr, interval=50)
+    g.set_checkpoint_storage("f16")
+    g16 = g.lin_adjoint(c["jts"], c["nt"], tr, interval=50)  # own sweep
+    g.check(g.lib.born_set_checkpoint_interval(g.h, 50))
+    lm = g.lin_forward(c["jts"], c["nt"], m)               # stores FP16
+    g16b = g.lin_adjoint(c["jts"], c["nt"], tr, interval=50)
+    assert g.lib.born_checkpoints_reused(g.h) == 1
+    assert np.array_equal(g16, g16b)
+    o = po.PortProp64()
+    po.run_case(o, c, which="none")
+    o.transferReceiverFunc(c["rec_nx"], c["rec_ny"], c["nt_big"],
+                           c["locs_r"], np.zeros(c["rec_in"].shape))
+    want = o.lin_adjoint(c["jts"], tr, c["nt"])
+    e16, e32 = rel(g16, want), rel(g32, want)
+    print(f"gradient vs FP64: FP16 checkpoints {e16:.3e}, FP32 {e32:.3e}")
+    assert e32 <= 1e-5
+    assert e16 <= 1e-3, e16
+    a = float(np.vdot(lm.astype(np.float64), tr.astype(np.float64)))
+    b = float(np.vdot(m.astype(np.float64), g16.astype(np.float64)))
+    print(f"dot test with FP16 checkpoints {abs(a - b) / abs(a):.3e}")
+    assert abs(a - b) <= 1e-3 * abs(a)
