@@ -6,7 +6,8 @@ seeded cases and stores inputs and outputs in ``tests/golden/*.npz``.  Needs
 the reference sources (present only where the fixtures are made); the
 fixtures themselves travel with the repository.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py           # every fixture
+    python tests/golden/make_golden.py solver    # solver_ref.npz only
 """
 import os
 import sys
@@ -66,5 +67,42 @@ def make_geometry():
 GEOMETRY_SEED = 0
 
 
+def make_solver():
+    """Outputs of the reference's own least-squares classes (lin_solver,
+    cgstep; compiled from its sources into oracle/_ref by oracle/Makefile):
+    the CG loop on a host problem (tests/cpp/pin_solver.cc) and the operator
+    adapter under those classes over a host stand-in of the C ABI
+    (tests/cpp/drive_solver.cc + fake_born.cc) on the problem
+    tests/test_solver_adapter.py uses."""
+    import subprocess
+    import tempfile
+    import pathlib
+    import test_solver_adapter as tsa
+    pin = po.ref_program("pin_solver_ref")
+    drive = po.ref_program("drive_solver_ref_fake")
+    if pin is None or drive is None:
+        sys.exit("reference sources not available: cannot make fixtures")
+    pin_out = subprocess.run([pin, "10"], capture_output=True, text=True,
+                             check=True).stdout
+    kw, m_true = tsa.fake_problem()
+    with tempfile.TemporaryDirectory() as d:
+        d = pathlib.Path(d)
+        tsa.write_problem(d, kw, m_true)
+        drive_out = subprocess.run([drive, str(d), "6", "1"],
+                                   capture_output=True, text=True,
+                                   check=True).stdout
+        model = np.fromfile(d / "model_solver.f32", np.float32)
+    np.savez_compressed(os.path.join(HERE, "solver_ref.npz"),
+                        pin_stdout=np.array(pin_out),
+                        adapter_stdout=np.array(drive_out),
+                        adapter_model=model)
+    print(pin_out)
+    print(drive_out)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["solver"]:
+        make_solver()
+    else:
+        main()
+        make_solver()

@@ -77,33 +77,51 @@ def parse(out):
     return res
 
 
-def test_restated_solver_matches_reference_solver(po, tmp_path):
-    ref = po.ref_program("pin_solver_ref")
-    if ref is None:
-        pytest.skip("reference solver not built (set SC17_BORN_REF)")
-    mine = build_restated(tmp_path, "pin_solver",
-                          [os.path.join(TCPP, "pin_solver.cc")])
-    a = subprocess.run([ref, "10"], capture_output=True, text=True,
-                       check=True).stdout
-    b = subprocess.run([mine, "10"], capture_output=True, text=True,
-                       check=True).stdout
-    assert "rr10 " in a and "dot_test 1" in a
-    assert a == b
+GOLDEN = os.path.join(ROOT, "tests", "golden", "solver_ref.npz")
 
 
-def test_adapter_under_reference_solver_cpu(po, tmp_path):
-    ref = po.ref_program("drive_solver_ref_fake")
-    if ref is None:
-        pytest.skip("reference solver not built (set SC17_BORN_REF)")
-    mine = build_restated(tmp_path, "drive_solver_fake",
-                          [os.path.join(TCPP, "drive_solver.cc"),
-                           os.path.join(TCPP, "fake_born.cc")])
+def fake_problem():
+    """The small problem the adapter runs on over the host stand-in."""
     from test_operator import setup_problem
     kw = setup_problem(seed=3, n=(6, 7, 8), nt_data=12, nshots=1)
     m_true = np.zeros(kw["velocity"].shape, np.float32)
     m_true.ravel()[::5] = 1.0
-    outs = []
-    for exe in (ref, mine):
+    return kw, m_true
+
+
+def test_restated_solver_matches_reference_solver(po, tmp_path):
+    """Against the reference classes' output stored by
+    tests/golden/make_golden.py, and against the live build where the
+    reference's sources are present."""
+    mine = build_restated(tmp_path, "pin_solver",
+                          [os.path.join(TCPP, "pin_solver.cc")])
+    b = subprocess.run([mine, "10"], capture_output=True, text=True,
+                       check=True).stdout
+    want = str(np.load(GOLDEN)["pin_stdout"])
+    assert "rr10 " in want and "dot_test 1" in want
+    assert b == want
+    ref = po.ref_program("pin_solver_ref")
+    if ref is not None:
+        a = subprocess.run([ref, "10"], capture_output=True, text=True,
+                           check=True).stdout
+        assert a == b
+
+
+def test_adapter_under_reference_solver_cpu(po, tmp_path):
+    """The adapter over the host stand-in: under the restated classes it
+    prints what it printed under the reference's own (stored fixture, and
+    the live build where the reference's sources are present)."""
+    mine = build_restated(tmp_path, "drive_solver_fake",
+                          [os.path.join(TCPP, "drive_solver.cc"),
+                           os.path.join(TCPP, "fake_born.cc")])
+    kw, m_true = fake_problem()
+    g = np.load(GOLDEN)
+    outs = [(parse(str(g["adapter_stdout"])), g["adapter_model"])]
+    exes = [mine]
+    ref = po.ref_program("drive_solver_ref_fake")
+    if ref is not None:
+        exes.append(ref)
+    for exe in exes:
         d = tmp_path / ("run_" + os.path.basename(exe))
         d.mkdir()
         write_problem(d, kw, m_true)
@@ -112,10 +130,12 @@ def test_adapter_under_reference_solver_cpu(po, tmp_path):
         assert r.returncode == 0, r.stderr[-2000:]
         outs.append((parse(r.stdout),
                      np.fromfile(d / "model_solver.f32", np.float32)))
-    (a, ma), (b, mb) = outs
+    a, ma = outs[0]
     assert len(a["solver"]) == 7 and a["solver"][-1] < a["solver"][0]
-    assert a == b and a["dot_test"] == 1
-    assert np.array_equal(ma, mb)
+    assert a["dot_test"] == 1
+    for b, mb in outs[1:]:
+        assert a == b
+        assert np.array_equal(ma, mb)
 
 
 def test_adapter_compiles_and_links_against_library(born, tmp_path):
