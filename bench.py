@@ -585,6 +585,7 @@ def run_exact(args):
                               case["locs_r"], rec)
     prop.check(prop.lib.born_set_reflectivity(prop.h, born.fptr(case["refl"])))
     prop.check(prop.lib.born_set_checkpoint_interval(prop.h, interval))
+    prop.set_checkpoint_storage(args.ckpt_storage)
     stream = torch.cuda.ExternalStream(prop.stream, device=0)
 
     def step(ev=None):
@@ -627,6 +628,17 @@ def run_exact(args):
     sweep_ms, recomp_ms, rev_ms, div_ms = prop.phase_times()
     reused = bool(prop.lib.born_checkpoints_reused(prop.h))
     prop.time_phases(False)
+    # FP16 checkpoints: the gradient's distance from the FP32-checkpoint one
+    ckpt_err = None
+    if args.ckpt_storage != "f32":
+        g16 = prop.get_image()
+        prop.set_checkpoint_storage("f32")
+        prop.zero_traces()
+        prop.lin_forward_device(jt, nt)
+        prop.lin_adjoint_device(jt, nt, interval)
+        g32 = prop.get_image()
+        ckpt_err = float(np.linalg.norm((g16 - g32).ravel()) /
+                         max(np.linalg.norm(g32.ravel()), 1e-30))
     cells = 2 * n_int * nt
     value = cells * args.steps / (t_ms / 1e3) / 1e9
     algo = n_int * (32 + 48 + (0 if reused else 16)) * nt + \
@@ -677,7 +689,10 @@ def run_exact(args):
                        "l2": "inputs larger than L2"},
             "algorithmic_bytes_per_step": int(algo),
             "roofline": roofline, "phases": phases,
-            "checkpoint_bytes": int(2 * nseg * n123 * 4),
+            "checkpoint_storage": args.ckpt_storage,
+            "gradient_rel_l2_vs_f32_checkpoints": ckpt_err,
+            "checkpoint_bytes": int(2 * nseg * n123 *
+                                    (2 if args.ckpt_storage == "f16" else 4)),
             "segment_bytes": int(interval * n123 * 4),
             "clocks": clk.summary(), "gpu_launches": launches}
     print(json.dumps(line), flush=True)
@@ -944,6 +959,8 @@ def main():
                          "checkpointed adjoint")
     ap.add_argument("--ckpt", type=int, default=50,
                     help="--adjoint exact: checkpoint interval (steps)")
+    ap.add_argument("--ckpt-storage", default="f32", choices=["f32", "f16"],
+                    help="--adjoint exact: checkpoint storage")
     ap.add_argument("--tile", type=int, default=-1)
     ap.add_argument("--zseg", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=2)

@@ -214,10 +214,12 @@ int born_set_checkpoint_interval(born_handle *h, int interval);
  * the background, else 0. */
 int born_checkpoints_reused(const born_handle *h);
 /* Storage of the exact adjoint's checkpoints: FP32 (default; the gradient is
- * the exact transpose), or FP16 with one power-of-two scale per checkpoint
- * level, 2^(ceil(log2 max|level|) - 15), chosen on the device (half the
- * memory; each segment is then recomputed from levels rounded to FP16, so
- * the gradient is the transpose to about FP16 rounding). */
+ * the exact transpose), or FP16 (half the memory): each checkpoint keeps
+ * the current level s_t and the difference s_{t-1} - s_t, each with its own
+ * power-of-two scale 2^(ceil(log2 max|v|) - 15) chosen on the device, and
+ * s_{t-1} is rebuilt in FP32 from the two; each segment is then recomputed
+ * from levels rounded to FP16, so the gradient is the transpose to about
+ * FP16 rounding. */
 #define BORN_CKPT_F32 0
 #define BORN_CKPT_F16 1
 int born_set_checkpoint_storage(born_handle *h, int storage);

@@ -1239,35 +1239,52 @@ int ensure_ckpt(born_handle *h, size_t levels) {
   return BORN_OK;
 }
 
-// Checkpoint level k <- src (a copy, or an FP16 snapshot with its scale).
-int store_ckpt(born_handle *h, size_t k, const float *src) {
+// Checkpoint k of the background: its two levels (old, cur) = (s_{t-1},
+// s_t) as stored at step t.  FP32: plain copies into levels 2k, 2k+1.
+// FP16: level 2k+1 holds cur and level 2k the difference old - cur, each
+// with its own power-of-two scale.  The difference is about omega dt of
+// the field, so it keeps FP16's relative precision at that small size:
+// the time derivative the leapfrog restarts from stays accurate, where two
+// independently rounded levels would differ by their rounding noise.
+int store_ckpt(born_handle *h, size_t k, const float *old, const float *cur) {
   const size_t n = (size_t)h->n123;
   if (h->ckpt_storage == BORN_CKPT_F16) {
     unsigned short *base = reinterpret_cast<unsigned short *>(h->ckpt);
-    CK(h, born::launch_snapshot_f16(src, (long long)n, h->ckpt_maxw,
-                                    base + k * n, h->ckpt_scale + k,
+    CK(h, born::launch_snapshot_f16(cur, nullptr, (long long)n, h->ckpt_maxw,
+                                    base + (2 * k + 1) * n,
+                                    h->ckpt_scale + 2 * k + 1, h->stream));
+    CK(h, born::launch_snapshot_f16(old, cur, (long long)n, h->ckpt_maxw,
+                                    base + 2 * k * n, h->ckpt_scale + 2 * k,
                                     h->stream));
-    h->launches += 2;
+    h->launches += 4;
     return BORN_OK;
   }
-  CK(h, cudaMemcpyAsync(h->ckpt + k * n, src, n * 4, cudaMemcpyDeviceToDevice,
-                        h->stream));
+  CK(h, cudaMemcpyAsync(h->ckpt + 2 * k * n, old, n * 4,
+                        cudaMemcpyDeviceToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(h->ckpt + (2 * k + 1) * n, cur, n * 4,
+                        cudaMemcpyDeviceToDevice, h->stream));
   return BORN_OK;
 }
 
-// dst <- checkpoint level k (FP32 values).
-int load_ckpt(born_handle *h, size_t k, float *dst) {
+// (old, cur) <- checkpoint k (FP32 values).
+int load_ckpt(born_handle *h, size_t k, float *old, float *cur) {
   const size_t n = (size_t)h->n123;
   if (h->ckpt_storage == BORN_CKPT_F16) {
     const unsigned short *base =
         reinterpret_cast<const unsigned short *>(h->ckpt);
-    CK(h, born::launch_restore_f16(base + k * n, (long long)n,
-                                   h->ckpt_scale + k, dst, h->stream));
-    h->launches++;
+    CK(h, born::launch_restore_f16(base + (2 * k + 1) * n, (long long)n,
+                                   h->ckpt_scale + 2 * k + 1, nullptr, cur,
+                                   h->stream));
+    CK(h, born::launch_restore_f16(base + 2 * k * n, (long long)n,
+                                   h->ckpt_scale + 2 * k, cur, old,
+                                   h->stream));
+    h->launches += 2;
     return BORN_OK;
   }
-  CK(h, cudaMemcpyAsync(dst, h->ckpt + k * n, n * 4, cudaMemcpyDeviceToDevice,
-                        h->stream));
+  CK(h, cudaMemcpyAsync(old, h->ckpt + 2 * k * n, n * 4,
+                        cudaMemcpyDeviceToDevice, h->stream));
+  CK(h, cudaMemcpyAsync(cur, h->ckpt + (2 * k + 1) * n, n * 4,
+                        cudaMemcpyDeviceToDevice, h->stream));
   return BORN_OK;
 }
 }  // namespace
@@ -1301,8 +1318,7 @@ int born_lin_forward(born_handle *h, int jt, int nt, float *traces_out) {
   const float scale = 1 / (float)jt;
   for (int it = 0; it < nt; ++it) {
     if (every > 0 && it % every == 0) {
-      rc = store_ckpt(h, 2 * (size_t)(it / every), sp0);
-      if (!rc) rc = store_ckpt(h, 2 * (size_t)(it / every) + 1, sp1);
+      rc = store_ckpt(h, (size_t)(it / every), sp0, sp1);
       if (rc) return rc;
     }
     const int id = it / jt, ii = it - id * jt;
@@ -1389,8 +1405,7 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
     float *sp0 = h->f0, *sp1 = h->f1;
     for (int it = 0; it < nt; ++it) {
       if (it % interval == 0) {
-        rc = store_ckpt(h, 2 * (size_t)(it / interval), sp0);
-        if (!rc) rc = store_ckpt(h, 2 * (size_t)(it / interval) + 1, sp1);
+        rc = store_ckpt(h, (size_t)(it / interval), sp0, sp1);
         if (rc) return rc;
       }
       rc = model_step(sp0, sp1, it, nullptr);
@@ -1416,8 +1431,7 @@ int born_lin_adjoint(born_handle *h, int jt, int nt, int interval,
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int t0 = seg * interval, t1 = std::min(nt, t0 + interval);
     float *a0 = h->f0, *a1 = h->f1;
-    rc = load_ckpt(h, 2 * (size_t)seg, a0);
-    if (!rc) rc = load_ckpt(h, 2 * (size_t)seg + 1, a1);
+    rc = load_ckpt(h, (size_t)seg, a0, a1);
     if (rc) return rc;
     for (int it = t0; it < t1; ++it) {
       rc = model_step(a0, a1, it, h->gbuf + (size_t)(it - t0) * n);

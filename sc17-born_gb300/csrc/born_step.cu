@@ -75,51 +75,72 @@ __global__ void absmax_kernel(const float *x, long long n, unsigned int *out) {
   if ((threadIdx.x & 31) == 0) atomicMax(out, w);
 }
 
-// FP16 snapshot of an FP32 level: the power-of-two scale
-// 2^(ceil(log2 max|x|) - 15) (pow2_scale_for, from the maximum the absmax
-// kernel left in *maxw) keeps every stored value within FP16's finite
-// range; each value is x / scale (an exact division) rounded to the nearest
-// FP16, and the scale is recorded in *scale_out.
-__global__ void snapshot_f16_kernel(const float *x, long long n,
-                                    const unsigned int *maxw, __half *out,
-                                    float *scale_out) {
+// v_i = x_i, or x_i - y_i when y is given (a difference of two levels)
+__device__ __forceinline__ float snap_value(const float *x, const float *y,
+                                            long long i) {
+  return y ? __fsub_rn(x[i], y[i]) : x[i];
+}
+
+__global__ void absmax_snap_kernel(const float *x, const float *y,
+                                   long long n, unsigned int *out) {
+  float m = 0.f;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf(snap_value(x, y, i)));
+  const unsigned int w = __reduce_max_sync(0xffffffffu, __float_as_uint(m));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, w);
+}
+
+// FP16 snapshot of v (an FP32 level, or the difference of two): the
+// power-of-two scale 2^(ceil(log2 max|v|) - 15) (pow2_scale_for, from the
+// maximum absmax_snap_kernel left in *maxw) keeps every stored value
+// within FP16's finite range; each value is v / scale (an exact division)
+// rounded to the nearest FP16, and the scale is recorded in *scale_out.
+__global__ void snapshot_f16_kernel(const float *x, const float *y,
+                                    long long n, const unsigned int *maxw,
+                                    __half *out, float *scale_out) {
   const float scale = pow2_scale_for(__uint_as_float(*maxw));
   const float inv = 1.f / scale;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
-    out[i] = __float2half_rn(clamp_f16(x[i] * inv));
+    out[i] = __float2half_rn(clamp_f16(snap_value(x, y, i) * inv));
   if (blockIdx.x == 0 && threadIdx.x == 0) *scale_out = scale;
 }
 
+// x = stored value * scale (+ base, when given)
 __global__ void restore_f16_kernel(const __half *in, long long n,
-                                   const float *scale, float *x) {
+                                   const float *scale, const float *base,
+                                   float *x) {
   const float sc = *scale;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x)
-    x[i] = __half2float(in[i]) * sc;
+       i += (long long)gridDim.x * blockDim.x) {
+    const float v = __half2float(in[i]) * sc;
+    x[i] = base ? __fadd_rn(v, base[i]) : v;
+  }
 }
 
 }  // namespace
 
-cudaError_t launch_snapshot_f16(const float *x, long long n,
+cudaError_t launch_snapshot_f16(const float *x, const float *y, long long n,
                                 unsigned int *maxw, void *out, float *scale,
                                 cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(maxw, 0, sizeof(unsigned int), stream);
   if (e != cudaSuccess) return e;
-  e = launch_absmax(x, n, maxw, stream);
-  if (e != cudaSuccess) return e;
   const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 8);
+  absmax_snap_kernel<<<blocks, 256, 0, stream>>>(x, y, n, maxw);
   snapshot_f16_kernel<<<blocks, 256, 0, stream>>>(
-      x, n, maxw, static_cast<__half *>(out), scale);
+      x, y, n, maxw, static_cast<__half *>(out), scale);
   return cudaGetLastError();
 }
 
 cudaError_t launch_restore_f16(const void *in, long long n,
-                               const float *scale, float *x,
-                               cudaStream_t stream) {
+                               const float *scale, const float *base,
+                               float *x, cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
   const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 8);
   restore_f16_kernel<<<blocks, 256, 0, stream>>>(
-      static_cast<const __half *>(in), n, scale, x);
+      static_cast<const __half *>(in), n, scale, base, x);
   return cudaGetLastError();
 }
 

@@ -224,17 +224,18 @@ cudaError_t launch_level_copy(unsigned long long *lv, int dst, int src,
 // *out = max(*out, max |x[i]|) as float bits (out zeroed by the caller).
 cudaError_t launch_absmax(const float *x, long long n, unsigned int *out,
                           cudaStream_t stream);
-// Checkpoints of the exact adjoint in FP16: snapshot writes x (n floats) as
-// FP16 values with the power-of-two scale 2^(ceil(log2 max|x|) - 15) stored
-// in *scale (maxw: a device word the call uses to find max|x|); restore
-// writes the FP16 values times *scale back as FP32.  No host
+// Checkpoints of the exact adjoint in FP16: snapshot writes v = x (or
+// x - y when y is not null; n floats) as FP16 values with the power-of-two
+// scale 2^(ceil(log2 max|v|) - 15) stored in *scale (maxw: a device word the
+// call uses to find max|v|); restore writes the FP16 values times *scale
+// (plus base[i] when base is not null) back as FP32.  No host
 // synchronisation.
-cudaError_t launch_snapshot_f16(const float *x, long long n,
+cudaError_t launch_snapshot_f16(const float *x, const float *y, long long n,
                                 unsigned int *maxw, void *out, float *scale,
                                 cudaStream_t stream);
 cudaError_t launch_restore_f16(const void *in, long long n,
-                               const float *scale, float *x,
-                               cudaStream_t stream);
+                               const float *scale, const float *base,
+                               float *x, cudaStream_t stream);
 // out[i] = a[i] / v[i] over the whole grid (image of the exact adjoint).
 cudaError_t launch_divide(const float *a, const float *v, float *out,
                           long long n, cudaStream_t stream);
