@@ -139,7 +139,11 @@ struct StepParams {
 };
 
 constexpr unsigned int kErrWaitTimeout = 1u;
-constexpr int kZStages = 3;  // z-window ring depth (new planes, 2 ahead)
+constexpr int kZStages = 3;  // largest z-window ring depth (planes ahead)
+// z-ring depth of a mode (at most kZStages)
+constexpr int z_stages(int mode) {
+  return mode == kModeForward ? 3 : mode == kModeSource ? 3 : 3;
+}
 constexpr int kOStages = 3;  // largest output ring depth (planes 2 ahead)
 // output ring depth of a mode (at most kOStages): the forward step keeps two
 // stages so that a 64x8 tile fits four CTAs per SM (shared memory) instead

@@ -549,8 +549,9 @@ struct Layout {
   static constexpr uint32_t kOTx =
       M::kNF * T::kBoxRaw + centre_bytes<MODE, M::kMask, T>(true);
   static constexpr int kOSt = out_stages(MODE);  // output ring depth
+  static constexpr int kZSt = z_stages(MODE);     // z ring depth
   static constexpr size_t kSmem =
-      (size_t)kZStages * kZStage + (size_t)kOSt * kOStage + 128;
+      (size_t)kZSt * kZStage + (size_t)kOSt * kOStage + 128;
 };
 
 // Scales of one step's levels (16-bit storage), shared by the CTA.
@@ -587,7 +588,7 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   // z ring: centre tiles of the current levels, one per new plane
   unsigned char *zring = smem;
   // output ring: halo boxes and per-cell inputs of the output plane
-  unsigned char *oring = smem + kZStages * LY::kZStage;
+  unsigned char *oring = smem + LY::kZSt * LY::kZStage;
 
   const int tid = threadIdx.x;
   const int lx = tid % (TX / 4), ly = tid / (TX / 4);
@@ -612,7 +613,7 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   }
 
   if (tid == 0) {
-    for (int s = 0; s < kZStages; ++s) mbar_init(&zbars[s], 1);
+    for (int s = 0; s < LY::kZSt; ++s) mbar_init(&zbars[s], 1);
     for (int s = 0; s < LY::kOSt; ++s) mbar_init(&obars[s], 1);
     // a wait elsewhere already gave up: the whole CTA leaves untouched
     abort_flag = *reinterpret_cast<volatile unsigned int *>(p.err) != 0u;
@@ -666,7 +667,7 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   const int J = z1 - z0;                  // output planes
   auto issue_z = [&](int k) {
     const int plane = z0 - kRadius + k;
-    const int st = k % kZStages;
+    const int st = k % LY::kZSt;
     mbar_expect_tx(&zbars[st], LY::kZTx);
     unsigned char *dst = zring + st * LY::kZStage;
     if (M::kBoxA) tma_load_3d(dst, &maps.zc_a, xz, y0, plane, &zbars[st]);
@@ -695,7 +696,7 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   };
   if (tid == 0) {
     if (NF > 0)
-      for (int k = 0; k < min(K, kZStages); ++k) issue_z(k);
+      for (int k = 0; k < min(K, LY::kZSt); ++k) issue_z(k);
     for (int j = 0; j < min(J, LY::kOSt); ++j) issue_out(j);
   }
 
@@ -716,14 +717,14 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   constexpr int kUnroll = MODE == kModeAdjoint ? 1 : 3;
 #pragma unroll kUnroll
   for (int k = 0; k < K; ++k) {
-    const int st = k % kZStages;
+    const int st = k % LY::kZSt;
     const int j = k - 2 * kRadius;       // output index once k >= 8
     const int zo = z0 + j;
     const long long idx = (long long)zo * n12 + (long long)gy * n1 + gx;
 
     bool ok = true;
     if (NF > 0) {
-      ok = mbar_wait_bounded(&zbars[st], (uint32_t)((k / kZStages) & 1));
+      ok = mbar_wait_bounded(&zbars[st], (uint32_t)((k / LY::kZSt) & 1));
       // newest plane's centre enters the z window
       const unsigned char *sa = zring + st * LY::kZStage;
 #pragma unroll
@@ -913,15 +914,15 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
     if (abort_flag) break;
     if (tid == 0) {
       fence_proxy_async();
-      if (NF > 0 && k + kZStages < K) issue_z(k + kZStages);
+      if (NF > 0 && k + LY::kZSt < K) issue_z(k + LY::kZSt);
       if (j >= 0 && j + LY::kOSt < J) issue_out(j + LY::kOSt);
     }
   }
 
   if (abort_flag && tid == 0) {
     // drain whatever is still in flight (bounded) before the CTA retires
-    for (int s = 0; s < kZStages + LY::kOSt; ++s) {
-      uint64_t *b = s < kZStages ? &zbars[s] : &obars[s - kZStages];
+    for (int s = 0; s < LY::kZSt + LY::kOSt; ++s) {
+      uint64_t *b = s < LY::kZSt ? &zbars[s] : &obars[s - LY::kZSt];
       const uint64_t t0 = global_ns();
       while (!mbar_try_wait(b, 0) && !mbar_try_wait(b, 1) &&
              global_ns() - t0 < 100000000ull) {
