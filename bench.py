@@ -508,25 +508,49 @@ def e2e_measure(born, case, args, dev, cells_per_step, world):
         L.born_set_tiling(h, args.tile, args.zseg)
     field = nx * ny * nz * 4
 
-    def step():
+    calls = ("transfer_source_func", "transfer_vel_func1", "transfer_vel_func2",
+             "transfer_receiver_func", "source_prop", "image_zero",
+             "rtm_adjoint", "transfer_receiver_func(zeros)", "rtm_forward")
+    call_s = dict.fromkeys(calls, 0.0)
+
+    def step(timed=False):
+        # every entry point below returns after its host copies completed,
+        # so the wall time between two calls is that call's own time
+        tk = [time.perf_counter()]
+
+        def lap():
+            if timed:
+                tk.append(time.perf_counter())
         # rtm_zero_op::adjoint per shot (rtm_zero_op_3d.cc:249-282)
         L.transfer_source_func(9, case["nt_big"], born.iptr(locs_s), fp(src))
+        lap()
         L.transfer_vel_func1(nx, ny, nz, fp(vel1))
+        lap()
         L.transfer_vel_func2(nx, ny, nz, fp(vel2))
+        lap()
         L.transfer_receiver_func(case["rec_nx"], case["rec_ny"],
                                  case["nt_big"], born.iptr(locs_r), fp(rec_in))
+        lap()
         L.source_prop(nx, ny, nz, False, True, fp(p0), fp(p1), jt, 9, nt)
+        lap()
         img.zero_()
+        lap()
         L.rtm_adjoint(nx, ny, nz, jt, fp(p1), fp(p0), fp(img), 9, nt)
+        lap()
         # rtm_zero_op::forward per shot (rtm_zero_op_3d.cc:147-185)
         L.transfer_receiver_func(case["rec_nx"], case["rec_ny"],
                                  case["nt_big"], born.iptr(locs_r),
                                  fp(zeros_rec))
+        lap()
         L.rtm_forward(nx, ny, nz, jt, fp(refl), fp(rec_out), 9, nt,
                       case["nt_big"], case["rec_nx"], case["rec_ny"])
+        lap()
         rc = L.born_default_status()
         if rc != 0:
             raise RuntimeError(L.born_default_error().decode())
+        if timed:
+            for k, name in enumerate(calls):
+                call_s[name] += tk[k + 1] - tk[k]
 
     for _ in range(max(1, args.warmup)):
         step()
@@ -534,16 +558,39 @@ def e2e_measure(born, case, args, dev, cells_per_step, world):
     steps = max(1, args.e2e_steps)
     t0 = time.perf_counter()
     for _ in range(steps):
-        step()
+        step(timed=True)
     t = time.perf_counter() - t0
     t = barrier_max(t, world)
+    copy_rates = pinned_copy_gbps(vel1, dev)
     rec_bytes = case["rec_in"].size * 4
     h2d = (2 * field + case["src"].size * 4 + 2 * rec_bytes + field + field)
     d2h = 2 * field + field + rec_bytes
     return {"value": round(world * cells_per_step * steps / t / 1e9, 3),
             "unit": "Gcell-updates/s", "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "steps": steps,
-            "api": "gpu_funcs_3d.h entry points, pinned host buffers"}
+            "api": "gpu_funcs_3d.h entry points, pinned host buffers",
+            "host_call_ms": {k: round(v * 1e3 / steps, 2)
+                             for k, v in call_s.items()},
+            "pinned_copy_GBps": copy_rates}
+
+
+def pinned_copy_gbps(host, dev, reps=3):
+    """torch's own copies of one pinned field each way (CUDA events)."""
+    import torch
+    d = torch.empty(host.shape, dtype=host.dtype, device=dev)
+    out = {}
+    for name, dst, src in (("h2d", d, host), ("d2h", host, d)):
+        dst.copy_(src, non_blocking=True)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            dst.copy_(src, non_blocking=True)
+        b.record()
+        b.synchronize()
+        out[name] = round(reps * host.numel() * 4 / (a.elapsed_time(b) / 1e3)
+                          / 1e9, 1)
+    return out
 
 
 def run_exact(args):
