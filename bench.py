@@ -376,11 +376,13 @@ def run_gpu_arm(args):
         prop.synchronize()
         torch.cuda.synchronize()
     launches = prop.launches - launches0
-    tiles, tile_ms = {}, {}
+    tiles, tile_ms, zsegs = {}, {}, {}
     for mode, name in ((1, "forward"), (0, "source"), (2, "adjoint")):
         cfg, ms = prop.tuned_config(mode)
         tiles[name] = cfg
-        # per-tile ms per launch as the loop's own refinement measured them
+        zsegs[name] = prop.tuned_zseg(mode)
+        # per-tile ms per launch (best z segmentation) as the loop's own
+        # refinement measured them
         tile_ms[name] = [round(v, 4) for v in prop.loop_tile_ms(mode)]
     t_ms = start.elapsed_time(stop)
     t_ms = barrier_max(t_ms, world)
@@ -461,6 +463,7 @@ def run_gpu_arm(args):
             "shot_steps_per_s": round(world * nt * args.steps / (t_ms / 1e3),
                                       1),
             "roofline": roofline, "phases": phases, "tile_cfg": tiles,
+            "tile_zseg": zsegs,
             "tile_ms_per_launch": tile_ms,
             "clocks": clk.summary(), "gpu_launches": launches,
             "e2e": e2e, "cpu_baseline": cpu, "fused_fma": fused,

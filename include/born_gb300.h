@@ -402,9 +402,9 @@ int born_set_tiling(born_handle *h, int tile_cfg, int zseg);
 /* Autotuner: with enable != 0, times every tile configuration of each step
  * mode on the current grid now (needs the grid and both velocities) and
  * uses the fastest; time loops also tune a mode lazily on first use while
- * enabled and no fixed tiling is set, and a loop of 400 steps or more then
- * refines the choice on its own steps (every tile gives the same results;
- * born_loop_tile_ms reports what it measured).  enable = 0 turns both off.
+ * enabled and no fixed tiling is set, and loops of 400 steps or more then
+ * refine the tile and its z segments on their own steps (every tiling gives
+ * the same results; born_loop_tile_ms reports what they measured).  enable = 0 turns both off.
  * A new grid (born_create_space) clears every choice. */
 int born_autotune(born_handle *h, int enable);
 /* Tile configuration in use for a step mode (0 source, 1 rtm forward,
@@ -412,10 +412,17 @@ int born_autotune(born_handle *h, int enable);
  * tuner's time per launch. */
 int born_tuned_config(const born_handle *h, int mode, int *cfg,
                       float *ms_per_launch);
-/* Time loops of 400 steps or more refine a mode's tile on their own steps
- * (every tile gives the same results): ms[c] receives the time per launch
- * the last refinement of the mode measured for tile configuration c (0 when
- * not measured), for c < n, under the current storage. */
+/* z-segment depth (planes per CTA) that a step of the mode uses now on the
+ * current grid: the fixed one, else the one tuned with the tile, else the
+ * sizing rule's.  Negative BORN_E* on error. */
+int born_tuned_zseg(born_handle *h, int mode);
+/* Time loops of 400 steps or more refine a mode's tiling, tile and z
+ * segments together, on their own steps (every tiling gives the same
+ * results; a loop too short for the whole sweep leaves the rest to the next
+ * loop of the mode): ms[c] receives the time per launch the last complete
+ * refinement of the mode measured for tile configuration c with its best z
+ * segmentation (0 when not measured), for c < n, under the current
+ * storage. */
 int born_loop_tile_ms(const born_handle *h, int mode, float *ms, int n);
 /* Failure-detection self-test: launches one kernel whose bounded device
  * wait (the step kernels' wait on their TMA copies) waits on something that
@@ -448,6 +455,15 @@ long long born_kernel_launches(const born_handle *h);
  * reference (within a relative L2 of 1e-5 of it), fewer instructions per
  * cell.  The other loops keep the reference order. */
 #define BORN_STORE_F32_FUSED 3
+/* FP32 levels in the reference's operation order, and the rtm forward
+ * loop's Born coupling r += 1e-6 s img formed exactly as the reference's
+ * double expression (base/cpu_prop.cc:216-223, a double literal times float
+ * fields, rounded once to float): traces bit-identical to the reference
+ * instead of within about 2e-6 relative L2.  The coupling is evaluated in
+ * float arithmetic (exact products and sums plus a rounding-boundary test)
+ * and falls back to double for the few cells the test cannot decide.  Every
+ * other step is the BORN_STORE_F32 one. */
+#define BORN_STORE_F32_EXACT 4
 int born_set_storage(born_handle *h, int storage);
 int born_get_storage(const born_handle *h);
 /* Raw CUDA stream of the handle (cudaStream_t), for event timing. */

@@ -95,6 +95,7 @@ _SIGS = {
     "born_autotune": (C.c_int, [_vp, C.c_int]),
     "born_tuned_config": (C.c_int, [_vp, C.c_int, _ip, _fp]),
     "born_loop_tile_ms": (C.c_int, [_vp, C.c_int, _fp, C.c_int]),
+    "born_tuned_zseg": (C.c_int, [_vp, C.c_int]),
     "born_set_checkpoint_interval": (C.c_int, [_vp, C.c_int]),
     "born_set_checkpoint_storage": (C.c_int, [_vp, C.c_int]),
     "born_checkpoints_reused": (C.c_int, [_vp]),
@@ -277,12 +278,14 @@ class Handle:
     def autotune(self, enable: bool = True):
         self.check(self.lib.born_autotune(self.h, int(enable)))
 
-    STORAGE = {"f32": 0, "bf16": 1, "f16": 2, "f32fma": 3}
+    STORAGE = {"f32": 0, "bf16": 1, "f16": 2, "f32fma": 3, "f32exact": 4}
 
     def set_storage(self, storage: str = "f32"):
         """Storage of the wavefield levels: "f32" (reference operation
-        order), "f32fma" (FP32 levels, fused multiply-add stencil), "bf16" or
-        "f16" (16-bit values with a power-of-two scale per level, FP32
+        order), "f32exact" (as "f32", with the rtm forward loop's Born
+        coupling formed exactly as the reference's double expression),
+        "f32fma" (FP32 levels, fused multiply-add stencil), "bf16" or "f16"
+        (16-bit values with a power-of-two scale per level, FP32
         arithmetic)."""
         self.check(self.lib.born_set_storage(self.h, self.STORAGE[storage]))
 
@@ -297,9 +300,16 @@ class Handle:
                                               C.byref(ms)))
         return cfg.value, ms.value
 
+    def tuned_zseg(self, mode: int) -> int:
+        """z-segment depth (planes per CTA) a step of `mode` uses now."""
+        z = int(self.lib.born_tuned_zseg(self.h, mode))
+        self.check(min(z, 0))
+        return z
+
     def loop_tile_ms(self, mode: int):
-        """ms per launch of every tile configuration as the last in-loop
-        refinement of `mode` measured it (0.0: not measured)."""
+        """ms per launch of every tile configuration (with its best z
+        segmentation) as the last complete in-loop refinement of `mode`
+        measured it (0.0: not measured)."""
         n = int(self.lib.born_tile_config_count())
         out = (C.c_float * n)()
         self.check(self.lib.born_loop_tile_ms(self.h, mode, out, n))

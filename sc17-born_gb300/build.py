@@ -19,13 +19,13 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libborn_gb300.so")
 
 SOURCES = ["born_step.cu", "born_step_bf16.cu", "born_step_f16.cu",
-           "born_step_f32fused.cu",
+           "born_step_f32fused.cu", "born_step_f32exact.cu",
            "born_api.cu", "born_operator.cu", "born_batch.cu",
            "born_noalloc.cu", "born_velocity.cu", "born_stream.cu",
            "born_host.cc",
            "born_sepio.cc"]
 HEADERS = ["born_step.cuh", "born_step_impl.cuh", "born_host.h",
-           "born_internal.h"]
+           "born_internal.h", "born_couple.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -253,13 +253,33 @@ int get_map(born_handle *h, const void *buf, int cfg, int kind, int esize,
   return BORN_OK;
 }
 
+// z-segment depth of the sizing rule: segments sized so that the grid
+// covers every SM about twice, at least 16 planes deep.
+int rule_zseg(born_handle *h, int mode, bool pa, bool pb, int cfg,
+              long long tiles) {
+  const int nzi = h->n3 - 8;
+  int tx, ty;
+  born::tile_cfg_dims(cfg, &tx, &ty);
+  int sms = 148;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
+  const size_t smem =
+      born::step_smem_bytes(h->storage_for(mode), cfg, mode, pa, pb);
+  int per_sm = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
+  per_sm = std::min(per_sm, 2048 / ((tx / 4) * ty));
+  const long long target = 2ll * sms * per_sm;
+  long long nseg = std::max<long long>(1, (target + tiles - 1) / tiles);
+  nseg = std::min<long long>(nseg, std::max(1, nzi / 16));
+  return (int)((nzi + nseg - 1) / nseg);
+}
+
 // Tiling: the configured one, else the autotuned one for the mode, else
-// 64x16 tiles; z segments sized so that the grid covers every SM a few times.
+// 64x16 tiles; z segments as configured, else as tuned with the tile, else
+// by the sizing rule.
 void pick_tiling(born_handle *h, int mode, bool pa, bool pb, int *cfg,
                  int *zseg, int *tiles_x, int *tiles_y) {
-  int c = h->tile_cfg >= 0                ? h->tile_cfg
-          : h->tuned_cfg[h->storage][mode] >= 0 ? h->tuned_cfg[h->storage][mode]
-                                          : 0;
+  const int slot = h->storage_for(mode);
+  const int tuned = h->tuned_cfg[slot][mode];
+  const int c = h->tile_cfg >= 0 ? h->tile_cfg : tuned >= 0 ? tuned : 0;
   int tx, ty;
   born::tile_cfg_dims(c, &tx, &ty);
   *cfg = c;
@@ -270,17 +290,12 @@ void pick_tiling(born_handle *h, int mode, bool pa, bool pb, int *cfg,
     *zseg = std::min(h->zseg, nzi);
     return;
   }
-  int sms = 148;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device);
-  const size_t smem =
-      born::step_smem_bytes(h->storage_for(mode), c, mode, pa, pb);
-  int per_sm = (int)std::max<size_t>(1, (227 * 1024) / (smem + 1024));
-  per_sm = std::min(per_sm, 2048 / ((tx / 4) * ty));
-  const long long target = 2ll * sms * per_sm;
-  const long long tiles = (long long)(*tiles_x) * (*tiles_y);
-  long long nseg = std::max<long long>(1, (target + tiles - 1) / tiles);
-  nseg = std::min<long long>(nseg, std::max(1, nzi / 16));
-  *zseg = (int)((nzi + nseg - 1) / nseg);
+  const int nseg = h->tuned_nseg[slot][mode];
+  if (h->tile_cfg < 0 && tuned >= 0 && nseg > 0) {
+    *zseg = (nzi + nseg - 1) / nseg;
+    return;
+  }
+  *zseg = rule_zseg(h, mode, pa, pb, c, (long long)(*tiles_x) * (*tiles_y));
 }
 
 PointSet point_view(const DevPoints &dp, int id, int ii,
@@ -437,8 +452,8 @@ int tune_mode(born_handle *h, int mode) {
   cudaStreamSynchronize(h->stream);
   cudaFree(timg);
   if (rc) return rc;
-  h->tuned_cfg[h->storage][mode] = best;
-  h->tuned_ms[h->storage][mode] = best_ms;
+  h->tuned_cfg[h->storage_for(mode)][mode] = best;
+  h->tuned_ms[h->storage_for(mode)][mode] = best_ms;
   const size_t bytes = h->level_bytes();
   float *scratch[] = {h->f0, h->f1, h->r0, h->r1};
   for (float *b : scratch) CK(h, cudaMemsetAsync(b, 0, bytes, h->stream));
@@ -446,33 +461,68 @@ int tune_mode(born_handle *h, int mode) {
 }
 
 int ensure_tuned(born_handle *h, int mode) {
-  if (!h->autotune || h->tile_cfg >= 0 || h->tuned_cfg[h->storage][mode] >= 0)
+  if (!h->autotune || h->tile_cfg >= 0 ||
+      h->tuned_cfg[h->storage_for(mode)][mode] >= 0)
     return BORN_OK;
   return tune_mode(h, mode);
 }
 
-// Refines a mode's tile choice on the first steps of a long time loop.  Every
-// tile gives bit-identical results, so the loop's own steps are timed: from
-// the loop's second step (the adjoint's first step is a lighter variant),
-// the tiles take turns in groups of one untimed step (the first launch with
-// a tile pays for its descriptors and attributes on the host) and
-// kLoopGroup timed ones between CUDA events, kLoopRounds times; the loop
-// then goes on with the tile of the smallest group time, kept for later
-// loops of the same storage and mode.  The scratch tuner's launches differ
-// from a loop's (inactive points, fixed buffers) and picked a forward tile
-// that ran 3.4 % slower in the loop than the best one (368^3 grid).
+// Refines a mode's tiling on the steps of its long time loops.  Every
+// tiling gives bit-identical results, so the loops' own steps are timed.
+// The candidates are (tile, z segments) pairs: each tile with the sizing
+// rule's segments and with 3 to 16 segments per column of tiles (at least 8
+// planes each).  The segment count moves the grid's last partial wave of
+// CTAs: on a 368^3 grid the adjoint step on 64x8 tiles took 0.341 ms per
+// launch with the rule's 4 segments and 0.314 ms with 10, and the best pairs
+// of all three steps were 6-8 % faster than the best tile at the rule's
+// segments.  From a loop's second step (the adjoint's first step is a
+// lighter variant), candidates take turns in groups of one untimed step
+// (the first launch with a tiling pays for its descriptors and attributes
+// on the host) and kLoopGroup timed ones between CUDA events: one group per
+// candidate, then kLoopRounds - 1 more rounds over the kLoopTop fastest of
+// the first round.  A loop too short for the whole sweep times what fits
+// and the next loop of the same storage and mode goes on from there.  When
+// every group is timed, the loop continues with the candidate of the
+// smallest group time, kept for later loops.  The scratch tuner's launches
+// differ from a loop's (inactive points, fixed buffers) and picked a
+// forward tile that ran 3.4 % slower in the loop than the best one (368^3
+// grid).
 constexpr int kLoopGroup = 8, kLoopRounds = 3, kLoopMinSteps = 400;
+constexpr int kLoopSegs[] = {3, 4, 5, 6, 8, 10, 12, 16};
 
 class LoopTuner {
  public:
-  LoopTuner(born_handle *h, int mode, int nsteps) : h_(h), mode_(mode) {
-    if (!h->autotune || h->tile_cfg >= 0 || nsteps < kLoopMinSteps ||
-        h->loop_tuned[h->storage][mode])
+  LoopTuner(born_handle *h, int mode, int nsteps, bool pb)
+      : h_(h), mode_(mode), st_(h->storage_for(mode)) {
+    if (!h->autotune || h->tile_cfg >= 0 || h->zseg > 0 ||
+        nsteps < kLoopMinSteps || h->loop_tuned[st_][mode])
       return;
-    ncfg_ = std::min(born::tile_cfg_count(), born_handle::kMaxTileCfgs);
-    groups_ = ncfg_ * kLoopRounds;
-    if (1 + groups_ * (kLoopGroup + 1) >= nsteps) return;
-    ev_.assign(2 * groups_, nullptr);
+    const int ncfg = std::min(born::tile_cfg_count(), born_handle::kMaxTileCfgs);
+    const int nzi = h->n3 - 8;
+    for (int c = 0; c < ncfg; ++c) {
+      int tx, ty;
+      born::tile_cfg_dims(c, &tx, &ty);
+      const long long tiles = (long long)((h->n1 - 8 + tx - 1) / tx) *
+                              ((h->n2 - 8 + ty - 1) / ty);
+      std::vector<int> seen{rule_zseg(h, mode, true, pb, c, tiles)};
+      add(c, 0);
+      for (int ns : kLoopSegs) {
+        if (nzi / ns < 8) break;
+        const int zs = (nzi + ns - 1) / ns;
+        if (std::find(seen.begin(), seen.end(), zs) != seen.end()) continue;
+        seen.push_back(zs);
+        add(c, ns);
+      }
+    }
+    ncand_ = (int)cand_.size();
+    ntop_ = std::min(ncand_, (int)born_handle::kLoopTop);
+    total_ = ncand_ + ntop_ * (kLoopRounds - 1);
+    g0_ = h->lt_next[st_][mode];
+    if (g0_ == 0)
+      for (float &b : h->lt_best[st_][mode]) b = -1.f;
+    nloc_ = std::min(total_ - g0_, (nsteps - 2) / (kLoopGroup + 1));
+    if (nloc_ <= 0) return;
+    ev_.assign(2 * nloc_, nullptr);
     for (cudaEvent_t &e : ev_)
       if (cudaEventCreate(&e) != cudaSuccess) {
         release();
@@ -488,35 +538,85 @@ class LoopTuner {
   int before(int k) {
     if (!on_ || k < 1) return BORN_OK;
     const int g = (k - 1) / (kLoopGroup + 1), r = (k - 1) % (kLoopGroup + 1);
-    if (r == 1 && g < groups_)  // the group's timed steps start here
+    if (r == 1 && g < nloc_)  // the group's timed steps start here
       CK(h_, cudaEventRecord(ev_[2 * g], h_->stream));
     if (r != 0) return BORN_OK;
     if (g > 0) CK(h_, cudaEventRecord(ev_[2 * g - 1], h_->stream));
-    if (g < groups_) {
-      h_->tuned_cfg[h_->storage][mode_] = g % ncfg_;
+    if (g < nloc_) {
+      if (g0_ + g == ncand_) {
+        // first round complete: keep its fastest candidates
+        int rc = fold(g);
+        if (rc) return rc;
+        const float *best = h_->lt_best[st_][mode_];
+        std::vector<int> order(ncand_);
+        for (int i = 0; i < ncand_; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+          const float ta = best[a] < 0.f ? 3e38f : best[a];
+          const float tb = best[b] < 0.f ? 3e38f : best[b];
+          return ta < tb;
+        });
+        for (int i = 0; i < ntop_; ++i) h_->lt_top[st_][mode_][i] = order[i];
+      }
+      use(cand_of(g0_ + g));
       return BORN_OK;
     }
-    CK(h_, cudaEventSynchronize(ev_[2 * groups_ - 1]));
-    std::vector<float> best(ncfg_, -1.f);
-    for (int i = 0; i < groups_; ++i) {
-      float ms = 0.f;
-      CK(h_, cudaEventElapsedTime(&ms, ev_[2 * i], ev_[2 * i + 1]));
-      float &b = best[i % ncfg_];
-      if (b < 0.f || ms < b) b = ms;
-    }
-    int pick = 0;
-    for (int c = 1; c < ncfg_; ++c)
-      if (best[c] < best[pick]) pick = c;
-    for (int c = 0; c < ncfg_; ++c)
-      h_->loop_ms[h_->storage][mode_][c] = best[c] / kLoopGroup;
-    h_->tuned_cfg[h_->storage][mode_] = pick;
-    h_->tuned_ms[h_->storage][mode_] = best[pick] / kLoopGroup;
-    h_->loop_tuned[h_->storage][mode_] = true;
-    release();
-    return BORN_OK;
+    return finish();
   }
 
  private:
+  void add(int cfg, int nseg) {
+    if ((int)cand_.size() < born_handle::kMaxLoopCands)
+      cand_.push_back({cfg, nseg});
+  }
+  // candidate timed by global group G
+  int cand_of(int G) const {
+    return G < ncand_ ? G : h_->lt_top[st_][mode_][(G - ncand_) % ntop_];
+  }
+  void use(int i) {
+    h_->tuned_cfg[st_][mode_] = cand_[i].first;
+    h_->tuned_nseg[st_][mode_] = cand_[i].second;
+  }
+  // fold the times of this loop's groups [folded_, upto) into the handle
+  int fold(int upto) {
+    if (upto <= folded_) return BORN_OK;
+    CK(h_, cudaEventSynchronize(ev_[2 * upto - 1]));
+    float *best = h_->lt_best[st_][mode_];
+    for (int i = folded_; i < upto; ++i) {
+      float ms = 0.f;
+      CK(h_, cudaEventElapsedTime(&ms, ev_[2 * i], ev_[2 * i + 1]));
+      float &b = best[cand_of(g0_ + i)];
+      if (b < 0.f || ms < b) b = ms;
+    }
+    folded_ = upto;
+    return BORN_OK;
+  }
+  // every group of this loop is timed: go on with the best candidate so far
+  // (the final choice when the sweep is complete)
+  int finish() {
+    int rc = fold(nloc_);
+    if (rc) return rc;
+    const float *best = h_->lt_best[st_][mode_];
+    int pick = -1;
+    for (int i = 0; i < ncand_; ++i)
+      if (best[i] >= 0.f && (pick < 0 || best[i] < best[pick])) pick = i;
+    if (pick >= 0) {
+      use(pick);
+      h_->tuned_ms[st_][mode_] = best[pick] / kLoopGroup;
+    }
+    h_->lt_next[st_][mode_] = g0_ + nloc_;
+    if (g0_ + nloc_ >= total_) {
+      float *tile_ms = h_->loop_ms[st_][mode_];
+      for (int c = 0; c < born_handle::kMaxTileCfgs; ++c) tile_ms[c] = 0.f;
+      for (int i = 0; i < ncand_; ++i) {
+        float &t = tile_ms[cand_[i].first];
+        const float ms = best[i] / kLoopGroup;
+        if (best[i] >= 0.f && (t == 0.f || ms < t)) t = ms;
+      }
+      h_->loop_tuned[st_][mode_] = true;
+    }
+    release();
+    return BORN_OK;
+  }
   void release() {
     for (cudaEvent_t e : ev_)
       if (e) cudaEventDestroy(e);
@@ -524,9 +624,10 @@ class LoopTuner {
     on_ = false;
   }
   born_handle *h_;
-  int mode_;
-  int ncfg_ = 0, groups_ = 0;
+  int mode_, st_;
+  int ncand_ = 0, ntop_ = 0, total_ = 0, g0_ = 0, nloc_ = 0, folded_ = 0;
   bool on_ = false;
+  std::vector<std::pair<int, int>> cand_;  // (tile configuration, segments)
   std::vector<cudaEvent_t> ev_;
 };
 
@@ -771,6 +872,10 @@ int born_create_space(born_handle *h, float d1, float d2, float d3, float bc_a,
     return fail(h, BORN_EINVAL, "spacings must be positive");
   int rc = set_device(h);
   if (rc) return rc;
+  // tile choices depend on the grid only: a new space over the same grid
+  // (the next operator of a job) keeps them
+  const bool same_grid =
+      h->have_space && nx == h->n1 && ny == h->n2 && nz == h->n3;
   cudaStreamSynchronize(h->stream);
   free_fields(h);
   h->src.release();
@@ -797,7 +902,7 @@ int born_create_space(born_handle *h, float d1, float d2, float d3, float bc_a,
   h->have_space = true;
   h->generation++;
   h->bg_gen++;
-  h->reset_tuning();  // tile choices are per grid
+  if (!same_grid) h->reset_tuning();
   return BORN_OK;
 }
 
@@ -886,7 +991,7 @@ int born_source_prop(born_handle *h, int jts, int nt, float *p0_out,
   }
   float *p0 = h->s0, *p1 = h->s1;
   const float scale = 1 / (float)jts;
-  LoopTuner tuner(h, kModeSource, nt + 1);
+  LoopTuner tuner(h, kModeSource, nt + 1, false);
   for (int it = 0; it <= nt; ++it) {
     rc = tuner.before(it);
     if (rc) return rc;
@@ -961,7 +1066,7 @@ int born_rtm_adjoint(born_handle *h, int jtd, int nt, int swap,
   float *rp0 = h->r0, *rp1 = h->r1;
   const float scale = -1 / (float)h->jt;
   PointSet pending = point_view(h->src, 0, 0, h->tab_s, 0.f, false);
-  LoopTuner tuner(h, kModeAdjoint, nt);
+  LoopTuner tuner(h, kModeAdjoint, nt, true);
   for (int it = nt - 1; it >= 0; --it) {
     rc = tuner.before(nt - 1 - it);
     if (rc) return rc;
@@ -1081,7 +1186,7 @@ int born_rtm_forward(born_handle *h, int jt, int nt, float *traces_out) {
   }
   float *sp0 = h->f0, *sp1 = h->f1, *rp0 = h->r0, *rp1 = h->r1;
   const float scale = 1 / (float)jt;
-  LoopTuner tuner(h, kModeForward, nt);
+  LoopTuner tuner(h, kModeForward, nt, true);
   for (int it = 0; it < nt; ++it) {
     rc = tuner.before(it);
     if (rc) return rc;
@@ -1584,15 +1689,26 @@ int born_tuned_config(const born_handle *h, int mode, int *cfg,
                       float *ms_per_launch) {
   if (!h || mode < 0 || mode > 5) return BORN_EINVAL;
   if (cfg)
-    *cfg = h->tile_cfg >= 0 ? h->tile_cfg : h->tuned_cfg[h->storage][mode];
-  if (ms_per_launch) *ms_per_launch = h->tuned_ms[h->storage][mode];
+    *cfg = h->tile_cfg >= 0 ? h->tile_cfg
+                            : h->tuned_cfg[h->storage_for(mode)][mode];
+  if (ms_per_launch) *ms_per_launch = h->tuned_ms[h->storage_for(mode)][mode];
   return BORN_OK;
+}
+
+int born_tuned_zseg(born_handle *h, int mode) {
+  if (!h || mode < 0 || mode > 5) return BORN_EINVAL;
+  if (!h->have_space) return fail(h, BORN_ESTATE, "no grid");
+  int cfg, zseg, tx, ty;
+  const bool pb = mode == kModeForward || mode == kModeAdjoint ||
+                  mode == born::kModeBornLin;
+  pick_tiling(h, mode, true, pb, &cfg, &zseg, &tx, &ty);
+  return zseg;
 }
 
 int born_loop_tile_ms(const born_handle *h, int mode, float *ms, int n) {
   if (!h || mode < 0 || mode > 5 || !ms || n < 0) return BORN_EINVAL;
   for (int c = 0; c < n; ++c)
-    ms[c] = c < born_handle::kMaxTileCfgs ? h->loop_ms[h->storage][mode][c]
+    ms[c] = c < born_handle::kMaxTileCfgs ? h->loop_ms[h->storage_for(mode)][mode][c]
                                           : 0.f;
   return BORN_OK;
 }
@@ -1644,7 +1760,8 @@ int born_set_storage(born_handle *h, int storage) {
   int rc = check_ready(h);
   if (rc) return rc;
   if (storage != BORN_STORE_F32 && storage != BORN_STORE_BF16 &&
-      storage != BORN_STORE_F16 && storage != BORN_STORE_F32_FUSED)
+      storage != BORN_STORE_F16 && storage != BORN_STORE_F32_FUSED &&
+      storage != BORN_STORE_F32_EXACT)
     return fail(h, BORN_EINVAL, "unknown storage %d", storage);
   if (born::storage_16bit(storage) && h->n1 % 8 != 0)
     return fail(h, BORN_EINVAL,

@@ -86,25 +86,41 @@ struct born_handle {
   // autotuner: best tile configuration per storage and step mode (-1: not
   // tuned yet)
   bool autotune = true;
-  int tuned_cfg[4][6] = {{-1, -1, -1, -1, -1, -1},
-                         {-1, -1, -1, -1, -1, -1},
-                         {-1, -1, -1, -1, -1, -1},
-                         {-1, -1, -1, -1, -1, -1}};
-  float tuned_ms[4][6] = {};
+  static constexpr int kNS = born::kNumStorages;
+  int tuned_cfg[kNS][6] = {{-1, -1, -1, -1, -1, -1},
+                           {-1, -1, -1, -1, -1, -1},
+                           {-1, -1, -1, -1, -1, -1},
+                           {-1, -1, -1, -1, -1, -1},
+                           {-1, -1, -1, -1, -1, -1}};
+  float tuned_ms[kNS][6] = {};
   // tile choice refined on a time loop's own steps (LoopTuner in
   // born_api.cu), per storage and step mode
-  bool loop_tuned[4][6] = {};
-  // ms per launch of every tile as the last refinement measured it (0: not
-  // measured)
+  bool loop_tuned[kNS][6] = {};
+  // ms per launch of every tile (its best z segmentation) as the last
+  // refinement measured it (0: not measured)
   static constexpr int kMaxTileCfgs = 8;
-  float loop_ms[4][6][kMaxTileCfgs] = {};
+  float loop_ms[kNS][6][kMaxTileCfgs] = {};
+  // z segments per column of tiles chosen with the tile (0: the sizing rule
+  // of pick_tiling)
+  int tuned_nseg[kNS][6] = {};
+  // refinement progress, kept across time loops so that loops shorter than
+  // the whole candidate sweep continue it: groups timed so far and the best
+  // group time (ms, -1 none) of every (tile, z segments) candidate
+  static constexpr int kMaxLoopCands = 64, kLoopTop = 8;
+  int lt_next[kNS][6] = {};
+  float lt_best[kNS][6][kMaxLoopCands];
+  // the candidates timed again after the first round (its fastest ones)
+  int lt_top[kNS][6][kLoopTop];
   void reset_tuning() {
-    for (int st = 0; st < 4; ++st)
+    for (int st = 0; st < kNS; ++st)
       for (int m = 0; m < 6; ++m) {
         tuned_cfg[st][m] = -1;
         tuned_ms[st][m] = 0.f;
+        tuned_nseg[st][m] = 0;
         loop_tuned[st][m] = false;
+        lt_next[st][m] = 0;
         for (int c = 0; c < kMaxTileCfgs; ++c) loop_ms[st][m][c] = 0.f;
+        for (int c = 0; c < kMaxLoopCands; ++c) lt_best[st][m][c] = -1.f;
       }
   }
   // wavefield level storage (born::Storage) and, for 16-bit storage, the
@@ -120,13 +136,16 @@ struct born_handle {
   }
   int level_esize() const { return born::storage_esize(storage); }
   bool lp() const { return born::storage_16bit(storage); }
-  // storage a step mode runs with: the fused FP32 arithmetic covers the
-  // source, forward and adjoint steps; the other modes keep the reference
-  // order
+  // storage a step mode runs with (and the slot of its tile choices): the
+  // fused FP32 arithmetic covers the source, forward and adjoint steps, the
+  // exact Born coupling the forward step; the other modes keep the
+  // reference order
   int storage_for(int mode) const {
-    return (storage == born::kStoreF32Fused && mode > born::kModeAdjoint)
-               ? born::kStoreF32
-               : storage;
+    if (storage == born::kStoreF32Fused && mode > born::kModeAdjoint)
+      return born::kStoreF32;
+    if (storage == born::kStoreF32Exact && mode != born::kModeForward)
+      return born::kStoreF32;
+    return storage;
   }
   long long launches = 0;
   int ntblock = 0;

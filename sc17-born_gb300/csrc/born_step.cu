@@ -173,6 +173,9 @@ size_t step_smem_bytes(int storage, int cfg, int mode, bool pa, bool pb) {
     case kStoreBF16: return step_smem_bf16(cfg, mode, pa, pb);
     case kStoreF16: return step_smem_f16(cfg, mode, pa, pb);
     case kStoreF32Fused: return step_smem_f32fused(cfg, mode, pa, pb);
+    case kStoreF32Exact:
+      return mode == kModeForward ? step_smem_f32exact(cfg, mode, pa, pb)
+                                  : step_smem_f32(cfg, mode, pa, pb);
     default: return step_smem_f32(cfg, mode, pa, pb);
   }
 }
@@ -190,6 +193,10 @@ cudaError_t launch_step(int storage, int mode, bool pa, bool pb, int cfg,
     case kStoreF16:
       if (!lp_mode(mode)) return cudaErrorInvalidValue;
       return launch_step_f16(mode, pa, pb, cfg, maps, p, s);
+    case kStoreF32Exact:
+      return mode == kModeForward
+                 ? launch_step_f32exact(mode, pa, pb, cfg, maps, p, s)
+                 : launch_step_f32(mode, pa, pb, cfg, maps, p, s);
     case kStoreF32Fused:
       if (!lp_mode(mode)) return cudaErrorInvalidValue;
       return launch_step_f32fused(mode, pa, pb, cfg, maps, p, s);
@@ -217,6 +224,13 @@ cudaError_t launch_step_batched(int storage, int mode, bool pa, bool pb,
       return launch_step_batched_f16(mode, pa, pb, cfg, shots,
                                                block_start, nshots, total, var,
                                                s);
+    case kStoreF32Exact:
+      if (mode == kModeForward)
+        return launch_step_batched_f32exact(mode, pa, pb, cfg, shots,
+                                            block_start, nshots, total, var,
+                                            s);
+      return launch_step_batched_f32(mode, pa, pb, cfg, shots, block_start,
+                                     nshots, total, var, s);
     case kStoreF32Fused:
       return launch_step_batched_f32fused(mode, pa, pb, cfg, shots,
                                           block_start, nshots, total, var, s);

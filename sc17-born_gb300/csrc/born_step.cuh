@@ -93,7 +93,8 @@ struct PointSet {
 // multiply-adds; with 16-bit storage the stencil still accumulates in FP32
 // (fused) and every stored level carries its own power-of-two scale.
 enum Storage : int { kStoreF32 = 0, kStoreBF16 = 1, kStoreF16 = 2,
-                     kStoreF32Fused = 3 };
+                     kStoreF32Fused = 3, kStoreF32Exact = 4,
+                     kNumStorages = 5 };
 inline bool storage_16bit(int st) {
   return st == kStoreBF16 || st == kStoreF16;
 }

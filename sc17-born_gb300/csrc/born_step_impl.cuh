@@ -1,7 +1,7 @@
 // Templated body of the fused time-step kernels (design in born_step.cuh).
 // Included by born_step.cu (FP32 storage, reference order),
-// born_step_bf16.cu, born_step_f16.cu and born_step_f32fused.cu so that the
-// storage families compile in parallel; each includer instantiates its
+// born_step_bf16.cu, born_step_f16.cu, born_step_f32fused.cu and
+// born_step_f32exact.cu so that the storage families compile in parallel; each includer instantiates its
 // storage type with BORN_DEFINE_STORAGE_ENTRY.
 #pragma once
 #include <cuda_bf16.h>
@@ -9,6 +9,7 @@
 
 #include <atomic>
 
+#include "born_couple.h"
 #include "born_step.cuh"
 
 namespace born {
@@ -109,7 +110,9 @@ struct Store {
   static constexpr bool kLow = ST == kStoreBF16 || ST == kStoreF16;
   static constexpr int kBytes = kLow ? 2 : 4;
   // fused multiply-add arithmetic (every storage but the reference order)
-  static constexpr bool kFused = ST != kStoreF32;
+  static constexpr bool kFused = ST != kStoreF32 && ST != kStoreF32Exact;
+  // the Born coupling formed as the reference's double expression
+  static constexpr bool kExact = ST == kStoreF32Exact;
 };
 
 // Four consecutive values starting at element `e` of a shared tile.
@@ -506,6 +509,12 @@ struct Tile {
   static constexpr int kBoxBytes = (kBoxRaw + 127) / 128 * 128;
   static constexpr int kCRaw = TX * TY * 4;       // FP32 centre tile
   static constexpr int kCBytes = (kCRaw + 127) / 128 * 128;
+  // whole warps (the level maxima reduce over full warps); TMA boxes of
+  // whole 16-byte rows starting on 16-byte boundaries for both element
+  // sizes (tile origins are multiples of TX after the 4-cell halo)
+  static_assert(kThreads % 32 == 0, "tile threads must fill whole warps");
+  static_assert(TX % 8 == 0 && TX + 2 * kRadius <= 256 && TY + 2 * kRadius <= 256,
+                "tile width must keep TMA rows 16-byte aligned");
 };
 
 // centre slots that hold levels of the propagated fields (field storage)
@@ -874,12 +883,20 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
           if (p.pa.active) inject_row(p.pa, n1, n2, zo, gy, gx, na);
           if (MODE == kModeForward) {
             // Born coupling r += 1e-6 s img, then extraction from r
+            if constexpr (Store<ST>::kExact) {
 #pragma unroll
-            for (int h = 0; h < 2; ++h)
-              set_cells2(nb, h,
-                        add2(cells2(nb, h),
-                             mulx(mulx(pk2(1e-6f, 1e-6f), cells2(na, h)),
-                                  cells2(im, h))));
+              for (int jj = 0; jj < 4; ++jj)
+                set_comp(nb, jj,
+                         couple::couple_exact(comp(nb, jj), comp(na, jj),
+                                              comp(im, jj), nullptr));
+            } else {
+#pragma unroll
+              for (int h = 0; h < 2; ++h)
+                set_cells2(nb, h,
+                          add2(cells2(nb, h),
+                               mulx(mulx(pk2(1e-6f, 1e-6f), cells2(na, h)),
+                                    cells2(im, h))));
+            }
           }
           if (MODE == kModeForward || MODE == kModeBornLin) {
             if (p.pb.active) extract_row(p.pb, n1, n2, zo, gy, gx, nb);
@@ -1013,6 +1030,9 @@ __global__ void __launch_bounds__(Tile<TX, TY, 4>::kThreads)
 struct TileCfg {
   int tx, ty;
 };
+// (24x16 and 40x16 tiles, which divide a 360-cell interior exactly, ran
+// slower than 64x8 in every loop on a 368^3 grid: forward 0.339 and 0.314
+// ms per launch against 0.266, adjoint 0.380 and 0.371 against 0.314)
 constexpr TileCfg kTileCfgs[] = {{64, 16}, {32, 16}, {32, 32}, {64, 8},
                                  {32, 8}};
 constexpr int kNumTileCfgs = sizeof(kTileCfgs) / sizeof(kTileCfgs[0]);
@@ -1065,29 +1085,41 @@ cudaError_t launch_t_batched(const BatchShot *shots, const int *block_start,
 }
 
 // Dispatch over (mode, pa, pb) for one tile shape; F::go is instantiated
-// for every variant (FP32 storage: every mode; 16-bit: source, forward and
-// adjoint).
+// for every variant (FP32 storage: every mode; 16-bit and fused FP32:
+// source, forward and adjoint; exact coupling: the forward step).
 template <int ST, int TX, int TY, class F>
 auto dispatch(int mode, bool pa, bool pb, F f) {
-  if constexpr (ST == kStoreF32) {
-    switch (mode) {
-      case kModeModel: return f.template go<ST, kModeModel, true, false, TX, TY>();
-      case kModeBornLin:
-        return f.template go<ST, kModeBornLin, true, true, TX, TY>();
-      case kModeBornAdj:
-        return f.template go<ST, kModeBornAdj, true, false, TX, TY>();
-      default: break;
+  if constexpr (ST == kStoreF32Exact) {
+    // the only step with a Born coupling; the other steps of this storage
+    // are the FP32 ones
+    (void)mode;
+    (void)pa;
+    (void)pb;
+    return f.template go<ST, kModeForward, true, true, TX, TY>();
+  } else {
+    if constexpr (ST == kStoreF32) {
+      switch (mode) {
+        case kModeModel:
+          return f.template go<ST, kModeModel, true, false, TX, TY>();
+        case kModeBornLin:
+          return f.template go<ST, kModeBornLin, true, true, TX, TY>();
+        case kModeBornAdj:
+          return f.template go<ST, kModeBornAdj, true, false, TX, TY>();
+        default: break;
+      }
     }
-  }
-  switch (mode) {
-    case kModeSource: return f.template go<ST, kModeSource, true, false, TX, TY>();
-    case kModeForward:
-      return f.template go<ST, kModeForward, true, true, TX, TY>();
-    default:
-      if (pa && pb) return f.template go<ST, kModeAdjoint, true, true, TX, TY>();
-      if (pa) return f.template go<ST, kModeAdjoint, true, false, TX, TY>();
-      if (pb) return f.template go<ST, kModeAdjoint, false, true, TX, TY>();
-      return f.template go<ST, kModeAdjoint, false, false, TX, TY>();
+    switch (mode) {
+      case kModeSource:
+        return f.template go<ST, kModeSource, true, false, TX, TY>();
+      case kModeForward:
+        return f.template go<ST, kModeForward, true, true, TX, TY>();
+      default:
+        if (pa && pb)
+          return f.template go<ST, kModeAdjoint, true, true, TX, TY>();
+        if (pa) return f.template go<ST, kModeAdjoint, true, false, TX, TY>();
+        if (pb) return f.template go<ST, kModeAdjoint, false, true, TX, TY>();
+        return f.template go<ST, kModeAdjoint, false, false, TX, TY>();
+    }
   }
 }
 
@@ -1151,6 +1183,7 @@ BORN_DECLARE_STORAGE_ENTRY(f32)
 BORN_DECLARE_STORAGE_ENTRY(bf16)
 BORN_DECLARE_STORAGE_ENTRY(f16)
 BORN_DECLARE_STORAGE_ENTRY(f32fused)
+BORN_DECLARE_STORAGE_ENTRY(f32exact)
 
 #define BORN_DEFINE_STORAGE_ENTRY(ST, NAME)                                  \
   cudaError_t launch_step_##NAME(int mode, bool pa, bool pb, int cfg,        \

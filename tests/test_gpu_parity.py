@@ -47,8 +47,11 @@ def test_gpu_matches_reference_fixture(gpu, po, path):
     check(got, out)
 
 
-@pytest.mark.parametrize("cfg", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("cfg", range(8))
 def test_gpu_matches_oracle_all_tile_configs(gpu, po, cfg):
+    # 48 interior columns: a partial second 32- or 64-wide tile
+    if cfg >= gpu.lib().born_tile_config_count():
+        pytest.skip("no such tile configuration")
     c = cases.make_case(31 + cfg, shape=(40, 44, 56), nt=60, jt=1,
                         sinc=po.sinc_table)
     prop = gpu.Gb300Prop()
