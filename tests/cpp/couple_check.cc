@@ -6,6 +6,7 @@
 //   wide    - every finite float exponent for r, s and m
 //   neartie - r + V within about 2^-49 |r| of a float rounding boundary
 //   tiny    - products and levels around the underflow thresholds
+//   edge    - results around the smallest normal floats
 // Prints one line per class: cases, mismatches, double fallbacks.
 // Build: g++ -O2 -std=c++17 -ffp-contract=off -fno-fast-math
 #include <cmath>
@@ -116,6 +117,14 @@ int main(int argc, char **argv) {
       check(t, r, rand_float(0, 60), rand_float(90, 140));
     }
     report("tiny", t);
+  }
+  {
+    // results around the smallest normal floats, where the scaled
+    // evaluation of small fields hands over to the double expression
+    Tally t;
+    for (long long i = 0; i < n; ++i)
+      check(t, rand_float(0, 6), rand_float(20, 100), rand_float(100, 140));
+    report("edge", t);
   }
   {
     // the sign of zero: r = -0/+0 with zero and nonzero products

@@ -35,7 +35,7 @@ def test_couple_exact_matches_double_expression(checker):
         name, n, bad, fb = line.split()
         rows[name] = (int(n), int(bad), int(fb))
     print(out.stdout, out.stderr)
-    assert set(rows) == {"field", "wide", "neartie", "tiny", "zeros"}
+    assert set(rows) == {"field", "wide", "neartie", "tiny", "edge", "zeros"}
     for name, (n, bad, fb) in rows.items():
         assert n > 0 and bad == 0, (name, n, bad, out.stderr)
     # the near-tie class exercises both outcomes of the boundary test

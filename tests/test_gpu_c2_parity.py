@@ -12,8 +12,9 @@ cpu_prop.cc:22-129):
   the oracle's restatement (sinc table, source and receiver cells, source
   traces, random-boundary and plain v^2 dt^2 models, reflectivity);
 * source levels and image are bit-identical, Born traces within 1e-5
-  relative L2 (the reference forms the 1e-6 Born coupling in double, this
-  build in float).
+  relative L2 under FP32 storage (the reference forms the 1e-6 Born
+  coupling in double, that storage in float) and bit-identical under the
+  exact-coupling storage (the same shot again, "f32exact").
 """
 import importlib.util
 import os
@@ -63,3 +64,11 @@ def test_c2_shot_matches_oracle(born, po):
     e = rel(got["traces"], want["traces"])
     assert np.linalg.norm(want["traces"]) > 0
     assert e <= 1e-5, e
+    prop = born.Gb300Prop(0)
+    nz, ny, nx = case["shape"]
+    prop.createSpace(case["d"], case["d"], case["d"], 50, .0005, .0005, nx,
+                     ny, nz)
+    prop.set_storage("f32exact")
+    got = po.run_case(prop, case)
+    for k in ("src_p0", "src_p1", "image", "traces"):
+        assert np.array_equal(got[k], want[k]), (k, rel(got[k], want[k]))
