@@ -399,6 +399,12 @@ int born_stream_mix_gbs(int reads, int writes, long long n, int reps,
  * the built-in choice) and z-segment depth (0 = automatic). */
 int born_tile_config_count(void);
 int born_set_tiling(born_handle *h, int tile_cfg, int zseg);
+/* Step launches with programmatic dependent launch (default on): each time
+ * step's grid may become resident while the previous step's last CTAs
+ * finish, and waits for that grid on the device before reading or writing
+ * anything, which hides the launch gap between steps.  enable = 0 launches
+ * every step plainly.  Results are the same either way. */
+int born_set_launch_overlap(born_handle *h, int enable);
 /* Autotuner: with enable != 0, times every tile configuration of each step
  * mode on the current grid now (needs the grid and both velocities) and
  * uses the fastest; time loops also tune a mode lazily on first use while

@@ -96,6 +96,7 @@ _SIGS = {
     "born_tuned_config": (C.c_int, [_vp, C.c_int, _ip, _fp]),
     "born_loop_tile_ms": (C.c_int, [_vp, C.c_int, _fp, C.c_int]),
     "born_tuned_zseg": (C.c_int, [_vp, C.c_int]),
+    "born_set_launch_overlap": (C.c_int, [_vp, C.c_int]),
     "born_set_checkpoint_interval": (C.c_int, [_vp, C.c_int]),
     "born_set_checkpoint_storage": (C.c_int, [_vp, C.c_int]),
     "born_checkpoints_reused": (C.c_int, [_vp]),
@@ -274,6 +275,10 @@ class Handle:
 
     def set_tiling(self, cfg: int = -1, zseg: int = 0):
         self.check(self.lib.born_set_tiling(self.h, cfg, zseg))
+
+    def set_launch_overlap(self, enable: bool = True):
+        """Programmatic dependent launch of the time steps (default on)."""
+        self.check(self.lib.born_set_launch_overlap(self.h, int(enable)))
 
     def autotune(self, enable: bool = True):
         self.check(self.lib.born_autotune(self.h, int(enable)))

@@ -298,6 +298,37 @@ void pick_tiling(born_handle *h, int mode, bool pa, bool pb, int *cfg,
   *zseg = rule_zseg(h, mode, pa, pb, c, (long long)(*tiles_x) * (*tiles_y));
 }
 
+// Tilings a mode is tuned over: (tile configuration, z segments per column
+// of tiles; 0 = the sizing rule) pairs, each tile with the rule's segments
+// and with 3 to 16 segments (at least 8 planes each), without repeating a
+// segment depth within a tile.
+constexpr int kTuneSegs[] = {3, 4, 5, 6, 8, 10, 12, 16};
+
+std::vector<std::pair<int, int>> tiling_candidates(born_handle *h, int mode,
+                                                   bool pb) {
+  std::vector<std::pair<int, int>> cand;
+  const int ncfg = std::min(born::tile_cfg_count(), born_handle::kMaxTileCfgs);
+  const int nzi = h->n3 - 8;
+  for (int c = 0; c < ncfg; ++c) {
+    int tx, ty;
+    born::tile_cfg_dims(c, &tx, &ty);
+    const long long tiles = (long long)((h->n1 - 8 + tx - 1) / tx) *
+                            ((h->n2 - 8 + ty - 1) / ty);
+    std::vector<int> seen{rule_zseg(h, mode, true, pb, c, tiles)};
+    cand.push_back({c, 0});
+    for (int ns : kTuneSegs) {
+      if (nzi / ns < 8) break;
+      const int zs = (nzi + ns - 1) / ns;
+      if (std::find(seen.begin(), seen.end(), zs) != seen.end()) continue;
+      seen.push_back(zs);
+      cand.push_back({c, ns});
+    }
+  }
+  if ((int)cand.size() > born_handle::kMaxLoopCands)
+    cand.resize(born_handle::kMaxLoopCands);
+  return cand;
+}
+
 PointSet point_view(const DevPoints &dp, int id, int ii,
                     const std::vector<float> &tab, float scale, bool use) {
   PointSet ps;
@@ -335,6 +366,7 @@ void base_params(born_handle *h, StepParams &p) {
   p.csum = cs;
   p.la = p.lb = born::LevelRefs{-1, -1, -1, 0u};
   p.vmax_a = p.vmax_b = p.imgmax = h->stat_dev;  // set per mode when used
+  p.overlap = h->overlap ? 1 : 0;
 }
 
 // One step launch.  a_cur / b_cur: current levels of the propagated fields
@@ -399,7 +431,7 @@ int tune_mode(born_handle *h, int mode) {
     cudaFree(timg);
     return fail(h, BORN_ECUDA, "autotuner setup failed");
   }
-  const int saved = h->tile_cfg;
+  const int saved = h->tile_cfg, saved_zseg = h->zseg;
   int best = -1;
   float best_ms = 0.f;
   int rc = BORN_OK;
@@ -408,15 +440,27 @@ int tune_mode(born_handle *h, int mode) {
     const void *reset[] = {h->f0, h->f1, h->r0, h->r1};
     rc = born_lp_prologue(h, h->stream, reset, 4);
   }
-  // interleaved sweeps over the tiles, best sweep average per tile: tiles
-  // 3-4 % apart in the time loop were confused by two sweeps of four timed
-  // launches (about 1.3 ms each on a 368^3 grid)
+  // interleaved sweeps over the tilings, best sweep average per tiling:
+  // tiles 3-4 % apart in the time loop were confused by two sweeps of four
+  // timed launches (about 1.3 ms each on a 368^3 grid).  The source, rtm
+  // adjoint and rtm forward loops refine tile and z segments on their own
+  // steps, so they start from the tiles at the sizing rule's segments; the
+  // exact pair's modes have no such refinement and take every candidate
+  // tiling here.
   constexpr int kSweeps = 3, kWarm = 2, kTimed = 8;
-  const int ncfg = born::tile_cfg_count();
-  std::vector<float> cfg_ms(ncfg, -1.f);
-  for (int sweep = 0; sweep < kSweeps * ncfg && !rc; ++sweep) {
-    const int cfg = sweep % ncfg;
-    h->tile_cfg = cfg;
+  auto cand = tiling_candidates(h, mode, pb);
+  if (mode <= kModeAdjoint)
+    cand.erase(std::remove_if(cand.begin(), cand.end(),
+                              [](const std::pair<int, int> &c) {
+                                return c.second != 0;
+                              }),
+               cand.end());
+  const int ncand = (int)cand.size(), nzi = h->n3 - 8;
+  std::vector<float> cand_ms(ncand, -1.f);
+  for (int sweep = 0; sweep < kSweeps * ncand && !rc; ++sweep) {
+    const int ci = sweep % ncand, ns = cand[ci].second;
+    h->tile_cfg = cand[ci].first;
+    h->zseg = ns > 0 ? (nzi + ns - 1) / ns : 0;
     StepParams p;
     base_params(h, p);
     p.a_out = h->f1;
@@ -439,21 +483,24 @@ int tune_mode(born_handle *h, int mode) {
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     ms /= (float)kTimed;
-    if (!rc && (cfg_ms[cfg] < 0.f || ms < cfg_ms[cfg])) cfg_ms[cfg] = ms;
+    if (!rc && (cand_ms[ci] < 0.f || ms < cand_ms[ci])) cand_ms[ci] = ms;
   }
-  for (int cfg = 0; cfg < ncfg; ++cfg)
-    if (cfg_ms[cfg] >= 0.f && (best < 0 || cfg_ms[cfg] < best_ms)) {
-      best = cfg;
-      best_ms = cfg_ms[cfg];
+  for (int ci = 0; ci < ncand; ++ci)
+    if (cand_ms[ci] >= 0.f && (best < 0 || cand_ms[ci] < best_ms)) {
+      best = ci;
+      best_ms = cand_ms[ci];
     }
   h->tile_cfg = saved;
+  h->zseg = saved_zseg;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaStreamSynchronize(h->stream);
   cudaFree(timg);
   if (rc) return rc;
-  h->tuned_cfg[h->storage_for(mode)][mode] = best;
-  h->tuned_ms[h->storage_for(mode)][mode] = best_ms;
+  const int slot = h->storage_for(mode);
+  h->tuned_cfg[slot][mode] = best >= 0 ? cand[best].first : 0;
+  h->tuned_nseg[slot][mode] = best >= 0 ? cand[best].second : 0;
+  h->tuned_ms[slot][mode] = best_ms;
   const size_t bytes = h->level_bytes();
   float *scratch[] = {h->f0, h->f1, h->r0, h->r1};
   for (float *b : scratch) CK(h, cudaMemsetAsync(b, 0, bytes, h->stream));
@@ -469,9 +516,8 @@ int ensure_tuned(born_handle *h, int mode) {
 
 // Refines a mode's tiling on the steps of its long time loops.  Every
 // tiling gives bit-identical results, so the loops' own steps are timed.
-// The candidates are (tile, z segments) pairs: each tile with the sizing
-// rule's segments and with 3 to 16 segments per column of tiles (at least 8
-// planes each).  The segment count moves the grid's last partial wave of
+// The candidates are tiling_candidates' (tile, z segments) pairs.  The
+// segment count moves the grid's last partial wave of
 // CTAs: on a 368^3 grid the adjoint step on 64x8 tiles took 0.341 ms per
 // launch with the rule's 4 segments and 0.314 ms with 10, and the best pairs
 // of all three steps were 6-8 % faster than the best tile at the rule's
@@ -488,7 +534,6 @@ int ensure_tuned(born_handle *h, int mode) {
 // forward tile that ran 3.4 % slower in the loop than the best one (368^3
 // grid).
 constexpr int kLoopGroup = 8, kLoopRounds = 3, kLoopMinSteps = 400;
-constexpr int kLoopSegs[] = {3, 4, 5, 6, 8, 10, 12, 16};
 
 class LoopTuner {
  public:
@@ -497,23 +542,7 @@ class LoopTuner {
     if (!h->autotune || h->tile_cfg >= 0 || h->zseg > 0 ||
         nsteps < kLoopMinSteps || h->loop_tuned[st_][mode])
       return;
-    const int ncfg = std::min(born::tile_cfg_count(), born_handle::kMaxTileCfgs);
-    const int nzi = h->n3 - 8;
-    for (int c = 0; c < ncfg; ++c) {
-      int tx, ty;
-      born::tile_cfg_dims(c, &tx, &ty);
-      const long long tiles = (long long)((h->n1 - 8 + tx - 1) / tx) *
-                              ((h->n2 - 8 + ty - 1) / ty);
-      std::vector<int> seen{rule_zseg(h, mode, true, pb, c, tiles)};
-      add(c, 0);
-      for (int ns : kLoopSegs) {
-        if (nzi / ns < 8) break;
-        const int zs = (nzi + ns - 1) / ns;
-        if (std::find(seen.begin(), seen.end(), zs) != seen.end()) continue;
-        seen.push_back(zs);
-        add(c, ns);
-      }
-    }
+    cand_ = tiling_candidates(h, mode, pb);
     ncand_ = (int)cand_.size();
     ntop_ = std::min(ncand_, (int)born_handle::kLoopTop);
     total_ = ncand_ + ntop_ * (kLoopRounds - 1);
@@ -564,10 +593,6 @@ class LoopTuner {
   }
 
  private:
-  void add(int cfg, int nseg) {
-    if ((int)cand_.size() < born_handle::kMaxLoopCands)
-      cand_.push_back({cfg, nseg});
-  }
   // candidate timed by global group G
   int cand_of(int G) const {
     return G < ncand_ ? G : h_->lt_top[st_][mode_][(G - ncand_) % ntop_];
@@ -1744,6 +1769,12 @@ int born_time_phases(born_handle *h, int enable) {
 int born_phase_times(const born_handle *h, float *ms, int n) {
   if (!h || !ms || n < 0) return BORN_EINVAL;
   for (int k = 0; k < n && k < 4; ++k) ms[k] = h->phase_ms[k];
+  return BORN_OK;
+}
+
+int born_set_launch_overlap(born_handle *h, int enable) {
+  if (!h) return BORN_EINVAL;
+  h->overlap = enable != 0;
   return BORN_OK;
 }
 

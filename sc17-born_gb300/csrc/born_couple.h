@@ -108,11 +108,11 @@ BORN_HD float reference_double(float r, float s, float m) {
 constexpr float kCHi = 0x1.0c6f7ap-20f;
 constexpr float kCLo = 0x1.6bdb1ap-49f;
 
-// (float)((double)r + 1e-6 * (double)s * (double)m); *fell_back (when not
-// null) reports whether the double expression was needed.  One float
-// evaluation per cell, the cases chosen by selects, so that the lanes of a
-// warp stay together; only the double fallback branches.
-BORN_HD float couple_exact(float r, float s, float m, bool *fell_back) {
+// (float)((double)r + 1e-6 * (double)s * (double)m) in float arithmetic,
+// or *fell_back = true when only the double expression decides it.  One
+// float evaluation per cell, the cases chosen by selects, so that the lanes
+// of a warp stay together.
+BORN_HD float couple_fast(float r, float s, float m, bool *fell_back) {
   // small fields (the faint tails ahead of a wavefront) are evaluated as
   // 2^64 s and 2^64 r: exact scalings that make the double expression
   // exactly 2^64 W, so the float evaluation scaled back is (float)W while
@@ -149,10 +149,31 @@ BORN_HD float couple_exact(float r, float s, float m, bool *fell_back) {
   const float res = zero ? fadd(r, fmul(fmul(kCHi, s), m))
                   : keep_r ? r
                   : fmul(R, inv);
-  const bool fb = !zero && !keep_r && !ok;
-  if (fell_back) *fell_back = fb;
-  if (fb) return reference_double(r, s, m);
+  *fell_back = !zero && !keep_r && !ok;
   return res;
+}
+
+#ifdef __CUDACC__
+// the double fallback out of line, so that the compiler cannot turn the
+// rare branch into double arithmetic on every cell (FP64 runs at a small
+// fraction of the FP32 rate on this GPU)
+static __device__ __noinline__ float couple_slow(float r, float s, float m) {
+  return reference_double(r, s, m);
+}
+#endif
+
+// the reference's coupling: the float evaluation, else the double one;
+// *fell_back (when not null) reports the fallback
+BORN_HD float couple_exact(float r, float s, float m, bool *fell_back) {
+  bool fb = false;
+  float v = couple_fast(r, s, m, &fb);
+  if (fell_back) *fell_back = fb;
+#ifdef __CUDA_ARCH__
+  if (fb) v = couple_slow(r, s, m);
+#else
+  if (fb) v = reference_double(r, s, m);
+#endif
+  return v;
 }
 
 }  // namespace couple

@@ -80,6 +80,9 @@ struct born_handle {
   bool host_sums_valid = false;
   unsigned long long host_sum0 = 0, host_sum1 = 0;
   int tile_cfg = -1, zseg = 0;
+  // step launches overlap the previous step's tail (programmatic dependent
+  // launch); born_set_launch_overlap
+  bool overlap = true;
   // bumped whenever device buffers or point sets are reallocated, so that
   // cached descriptors and graphs built over them can notice
   unsigned long long generation = 0;

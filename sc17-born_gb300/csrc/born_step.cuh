@@ -137,6 +137,10 @@ struct StepParams {
   float csum;              // |c0| + 2 sum |ci|: stencil gain per unit v^2 dt^2
   const unsigned int *vmax_a, *vmax_b;  // max v^2 dt^2 seen by A / B
   const unsigned int *imgmax;           // max |reflectivity| (Born coupling)
+  // host side only: launch with programmatic stream serialization (the
+  // kernel waits for the previous grid itself, griddepcontrol.wait)
+  int overlap;
+  int pad_;
 };
 
 constexpr unsigned int kErrWaitTimeout = 1u;

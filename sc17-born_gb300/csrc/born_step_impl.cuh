@@ -576,6 +576,12 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
                                           const StepParams &p, int tile,
                                           int seg) {
   const StepMaps &maps = *mp;
+  // programmatic dependent launch: the next step's grid may be scheduled
+  // from now on, and this grid touches global memory only once the previous
+  // one has completed and its writes are visible (levels, image, traces,
+  // error word); both are no-ops for a plain launch
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   using M = ModeTraits<MODE, PA, PB>;
   using T = Tile<TX, TY, Store<ST>::kBytes>;
   using LY = Layout<ST, MODE, PA, PB, TX, TY>;
@@ -884,11 +890,25 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
           if (MODE == kModeForward) {
             // Born coupling r += 1e-6 s img, then extraction from r
             if constexpr (Store<ST>::kExact) {
+              // float evaluation of every cell, the double expression out
+              // of line for the few the rounding test cannot decide
+              float4 nr = nb;
+              unsigned int slow = 0u;
 #pragma unroll
-              for (int jj = 0; jj < 4; ++jj)
-                set_comp(nb, jj,
-                         couple::couple_exact(comp(nb, jj), comp(na, jj),
-                                              comp(im, jj), nullptr));
+              for (int jj = 0; jj < 4; ++jj) {
+                bool fb;
+                set_comp(nr, jj, couple::couple_fast(comp(nb, jj), comp(na, jj),
+                                                     comp(im, jj), &fb));
+                slow |= (fb ? 1u : 0u) << jj;
+              }
+              if (slow) {
+                for (int jj = 0; jj < 4; ++jj)
+                  if (slow & (1u << jj))
+                    set_comp(nr, jj, couple::couple_slow(comp(nb, jj),
+                                                         comp(na, jj),
+                                                         comp(im, jj)));
+              }
+              nb = nr;
             } else {
 #pragma unroll
               for (int h = 0; h < 2; ++h)
@@ -1065,6 +1085,21 @@ cudaError_t launch_t(const StepMaps &maps, const StepParams &p,
   if (e != cudaSuccess) return e;
   const int nseg = (p.n3 - 2 * kRadius + p.zseg - 1) / p.zseg;
   dim3 grid(p.tiles_x * p.tiles_y, nseg);
+  if (p.overlap) {
+    // the grid's CTAs may become resident while the previous step's last
+    // CTAs finish; the kernel waits for that grid before reading anything
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(T::kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, maps, p);
+  }
   kern<<<grid, T::kThreads, smem, stream>>>(maps, p);
   return cudaGetLastError();
 }
