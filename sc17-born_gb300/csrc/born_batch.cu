@@ -27,6 +27,8 @@
 using born::BatchShot;
 using born::StepVar;
 
+struct BatchTuner;
+
 struct born_batch {
   std::vector<born_handle *> shots;
   int device = 0;
@@ -39,7 +41,14 @@ struct born_batch {
     int *d_start = nullptr;
     int total = 0, cfg = 0;
   };
-  std::map<std::tuple<int, int, int, int>, Table> tables;
+  std::map<std::tuple<int, int, int, int, int, int>, Table> tables;
+  // tiling of the batched steps per step mode: tile configuration and z
+  // segment depth in planes (-1 / 0: the first shot's tuned tile at every
+  // shot's sizing rule), refined on the first run of each loop (tuned[m])
+  int cur_cfg[6] = {-1, -1, -1, -1, -1, -1}, cur_zseg[6] = {};
+  bool tuned[6] = {};
+  struct BatchTuner *tuner = nullptr;
+  int tuner_k = 0;
   // recorded loops by (loop kind, nt, jt, parities of the source levels'
   // record slots); wr_after: the level write counts the loop leaves behind
   struct Graph {
@@ -53,6 +62,116 @@ struct born_batch {
   std::vector<unsigned long long> generations;
   long long launches = 0;        // kernels run on the batch stream
   long long graph_launches = 0;  // replays of recorded time loops
+};
+
+
+// In-loop tiling refinement of a batched time loop, the batch's counterpart
+// of the single-shot loops' refinement: one tile for every shot's CTAs and
+// one z-segment depth in planes for every shot (0: each shot's sizing
+// rule).  The first shot's own tuned tile had run the c4 batch (48 shots,
+// 600 steps) at 165.8 Gcell-updates/s; 32x16 tiles with 48-plane segments
+// ran it at 179.4.  On the first run of a loop the candidates take turns
+// from its second step, in groups of one untimed step (which builds the
+// candidate's shot table) and kBatchGroup timed steps between CUDA events:
+// one group each, then kBatchRounds - 1 rounds over the kBatchTop fastest;
+// the loop goes on with the fastest and later runs (recorded graphs) use
+// it.  Every tiling gives bit-identical results.
+constexpr int kBatchGroup = 4, kBatchRounds = 3, kBatchTop = 6;
+constexpr int kBatchZsegs[] = {0, 32, 48, 64, 96};
+
+struct BatchTuner {
+  born_batch *b;
+  int mode;
+  std::vector<std::pair<int, int>> cand;  // (tile configuration, planes)
+  std::vector<float> best;                // best group time, -1 none
+  std::vector<int> top;
+  std::vector<cudaEvent_t> ev;
+  int ntop = 0, total = 0, folded = 0;
+  bool on = false;
+
+  BatchTuner(born_batch *b_, int mode_, int nsteps) : b(b_), mode(mode_) {
+    for (int c = 0; c < born::tile_cfg_count(); ++c)
+      for (int z : kBatchZsegs) cand.push_back({c, z});
+    best.assign(cand.size(), -1.f);
+    ntop = std::min((int)cand.size(), kBatchTop);
+    total = (int)cand.size() + ntop * (kBatchRounds - 1);
+    if ((nsteps - 2) / (kBatchGroup + 1) < total) return;  // keep the default
+    ev.assign(2 * total, nullptr);
+    for (cudaEvent_t &e : ev)
+      if (cudaEventCreate(&e) != cudaSuccess) {
+        release();
+        return;
+      }
+    on = true;
+  }
+  ~BatchTuner() { release(); }
+  BatchTuner(const BatchTuner &) = delete;
+  BatchTuner &operator=(const BatchTuner &) = delete;
+
+  void release() {
+    for (cudaEvent_t e : ev)
+      if (e) cudaEventDestroy(e);
+    ev.clear();
+    on = false;
+  }
+  int cand_of(int g) const {
+    const int n = (int)cand.size();
+    return g < n ? g : top[(g - n) % ntop];
+  }
+  void use(int i) {
+    b->cur_cfg[mode] = cand[i].first;
+    b->cur_zseg[mode] = cand[i].second;
+  }
+  cudaError_t fold(int upto) {
+    if (upto <= folded) return cudaSuccess;
+    cudaError_t e = cudaEventSynchronize(ev[2 * upto - 1]);
+    for (int i = folded; i < upto && e == cudaSuccess; ++i) {
+      float ms = 0.f;
+      e = cudaEventElapsedTime(&ms, ev[2 * i], ev[2 * i + 1]);
+      float &t = best[cand_of(i)];
+      if (e == cudaSuccess && (t < 0.f || ms < t)) t = ms;
+    }
+    folded = upto;
+    return e;
+  }
+  // before launching the loop's step k (k = 0 for its first step)
+  cudaError_t before(int k) {
+    if (!on || k < 1) return cudaSuccess;
+    const int g = (k - 1) / (kBatchGroup + 1), r = (k - 1) % (kBatchGroup + 1);
+    if (r == 1 && g < total) return cudaEventRecord(ev[2 * g], b->stream);
+    if (r != 0) return cudaSuccess;
+    if (g > 0) {
+      cudaError_t e = cudaEventRecord(ev[2 * g - 1], b->stream);
+      if (e != cudaSuccess) return e;
+    }
+    if (g < total) {
+      if (g == (int)cand.size()) {  // first round done: keep its fastest
+        cudaError_t e = fold(g);
+        if (e != cudaSuccess) return e;
+        std::vector<int> order(cand.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+        std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+          const float tx = best[x] < 0.f ? 3e38f : best[x];
+          const float ty = best[y] < 0.f ? 3e38f : best[y];
+          return tx < ty;
+        });
+        top.assign(order.begin(), order.begin() + ntop);
+      }
+      use(cand_of(g));
+      return cudaSuccess;
+    }
+    return finish();
+  }
+  cudaError_t finish() {
+    if (!on) return cudaSuccess;
+    cudaError_t e = fold(total);
+    int pick = -1;
+    for (size_t i = 0; i < cand.size(); ++i)
+      if (best[i] >= 0.f && (pick < 0 || best[i] < best[pick])) pick = (int)i;
+    if (pick >= 0) use(pick);
+    release();
+    return e;
+  }
 };
 
 namespace {
@@ -72,6 +191,11 @@ void drop_cache(born_batch *b) {
   b->tables.clear();
   for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second.exec);
   b->graphs.clear();
+  for (int m = 0; m < 6; ++m) {  // tilings depend on the shots' grids
+    b->cur_cfg[m] = -1;
+    b->cur_zseg[m] = 0;
+    b->tuned[m] = false;
+  }
 }
 
 bool stale(born_batch *b) {
@@ -120,26 +244,33 @@ Levels levels_for(born_handle *h, int kind, int parity) {
 
 int build_table(born_batch *b, int mode, bool pa, bool pb, int kind,
                 born_batch::Table **out) {
-  auto key = std::make_tuple(mode, (int)pa, (int)pb, kind);
+  const int want_cfg = b->cur_cfg[mode], want_zseg = b->cur_zseg[mode];
+  auto key = std::make_tuple(mode, (int)pa, (int)pb, kind, want_cfg, want_zseg);
   auto it = b->tables.find(key);
   if (it != b->tables.end()) {
     *out = &it->second;
     return BORN_OK;
   }
   born_handle *h0 = b->shots[0];
-  int rc = born_ensure_tuned(h0, mode);
-  if (rc) return bfail(b, rc, "autotune failed");
-  int cfg0, zs, tx, ty;
-  born_pick_tiling(h0, mode, pa, pb, &cfg0, &zs, &tx, &ty);
+  int cfg0 = want_cfg;
+  if (cfg0 < 0) {
+    int rc = born_ensure_tuned(h0, mode);
+    if (rc) return bfail(b, rc, "autotune failed");
+    int zs, tx, ty;
+    born_pick_tiling(h0, mode, pa, pb, &cfg0, &zs, &tx, &ty);
+  }
+  int rc = BORN_OK;
   std::vector<BatchShot> host(b->shots.size());
   std::vector<int> start(b->shots.size() + 1, 0);
   for (size_t s = 0; s < b->shots.size(); ++s) {
     born_handle *h = b->shots[s];
-    const int saved = h->tile_cfg;
+    const int saved = h->tile_cfg, saved_zseg = h->zseg;
     h->tile_cfg = cfg0;  // one tile shape for the whole launch
+    if (want_zseg > 0) h->zseg = want_zseg;
     int cfg, zseg, tiles_x, tiles_y;
     born_pick_tiling(h, mode, pa, pb, &cfg, &zseg, &tiles_x, &tiles_y);
     h->tile_cfg = saved;
+    h->zseg = saved_zseg;
     BatchShot &bs = host[s];
     std::memset(&bs, 0, sizeof(bs));
     born_base_params(h, bs.params);
@@ -233,6 +364,9 @@ int prepare(born_batch *b, int mode, bool pa, bool pb, int kind) {
 // its own buffers (write_a / write_b: the step writes field A / B).
 int launch_batched(born_batch *b, int mode, bool pa, bool pb, int kind,
                    StepVar var, bool write_a, bool write_b) {
+  if (b->tuner && b->tuner->mode == mode &&
+      b->tuner->before(b->tuner_k++) != cudaSuccess)
+    return bfail(b, BORN_ECUDA, "batch tiling refinement failed");
   born_batch::Table *t = nullptr;
   int rc = build_table(b, mode, pa, pb, kind, &t);
   if (rc) return rc;
@@ -303,6 +437,29 @@ int run_loop(born_batch *b, int kind, int nt, int jt, F body) {
     drop_cache(b);
     for (size_t i = 0; i < b->shots.size(); ++i)
       b->generations[i] = b->shots[i]->generation;
+  }
+  // the first run of a loop refines its tiling on its own steps, uncaptured
+  // (tables for every candidate are built on the way); later runs record
+  // and replay it with the chosen tiling
+  const int mode = kind == kLoopSource    ? born::kModeSource
+                   : kind == kLoopAdjoint ? born::kModeAdjoint
+                                          : born::kModeForward;
+  if (!b->tuned[mode]) {
+    b->tuned[mode] = true;
+    born_handle *s0 = b->shots[0];
+    if (s0->autotune && s0->tile_cfg < 0 && s0->zseg == 0) {
+      BatchTuner t(b, mode, kind == kLoopSource ? nt + 1 : nt);
+      if (t.on) {
+        b->tuner = &t;
+        b->tuner_k = 0;
+        int rc = body(b);
+        b->tuner = nullptr;
+        if (rc) return rc;
+        if (t.finish() != cudaSuccess)
+          return bfail(b, BORN_ECUDA, "batch tiling refinement failed");
+        return BORN_OK;
+      }
+    }
   }
   if (!b->use_graph) return body(b);
   born_handle *h0 = b->shots[0];

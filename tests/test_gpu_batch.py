@@ -76,3 +76,40 @@ def test_batch_matches_single_shots(born, po, graph, jt, storage):
         assert batch.launches == steps
     assert batch.launches >= steps
     assert batch.graph_launches == (6 if graph else 0)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_tiling_refinement_keeps_results(born, po, graph):
+    """Loops of 200 steps or more refine the batch's (tile, z-segment depth)
+    on their first run, uncaptured; later runs record and replay the chosen
+    tiling.  Every run gives every shot its single-shot results."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no GPU")
+    nt = 200
+    want = []
+    for k, sh in enumerate(SHAPES):
+        p, c = setup_shot(born, po, 190 + k, sh, nt=nt)
+        want.append(single(p, c))
+    shots = [setup_shot(born, po, 190 + k, sh, nt=nt)
+             for k, sh in enumerate(SHAPES)]
+    batch = born.Batch([p for p, _ in shots], graph=graph)
+    c0 = shots[0][1]
+    for rep in range(3):  # tuning run, recording run, replay
+        for p, c in shots:
+            p.set_traces(c["rec_in"])
+        batch.source_prop(c0["jts"], c0["nt"])
+        batch.rtm_adjoint(c0["jts"], c0["nt"])
+        for p, _ in shots:
+            p.zero_traces()
+        batch.rtm_forward(c0["jts"], c0["nt"])
+        batch.synchronize()
+        for (p, c), (img, tr) in zip(shots, want):
+            assert np.array_equal(p.get_image(), img), rep
+            assert np.array_equal(p.get_traces(c["rec_in"]), tr), rep
+        if rep == 0:
+            # the first run of every loop timed the candidates instead of
+            # recording a graph
+            assert batch.graph_launches == 0
+    assert batch.graph_launches == (6 if graph else 0)
+    assert batch.launches == 3 * (3 * nt + 1)
