@@ -93,3 +93,20 @@ def test_new_space_on_same_grid_keeps_tuning(gpu, po):
     # another grid starts over
     p.createSpace(c["d"], c["d"], c["d"], 50, .0005, .0005, nx, ny, nz + 4)
     assert not any(complete(p))
+
+
+def test_launch_overlap_keeps_results(gpu, po):
+    """Programmatic dependent launch of the steps (default) and plain
+    launches give the same levels, image and traces, equal to the oracle."""
+    c = cases.make_case(79, shape=(40, 44, 56), nt=90, jt=2,
+                        sinc=po.sinc_table)
+    want = po.run_case(po.PortProp(), c)
+    got = {}
+    for overlap in (True, False):
+        p = gpu.Gb300Prop()
+        p.set_launch_overlap(overlap)
+        got[overlap] = po.run_case(p, c)
+    for k in ("src_p0", "src_p1", "image", "traces"):
+        assert np.array_equal(got[True][k], got[False][k]), k
+    for k in ("src_p0", "src_p1", "image"):
+        assert np.array_equal(got[True][k], want[k]), k
