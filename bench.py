@@ -414,6 +414,30 @@ def run_gpu_arm(args):
                           "leapfrog (born_set_storage BORN_STORE_F32_FUSED)"}
         prop.set_storage("f32")
 
+    # the same loops with the Born coupling formed exactly as the
+    # reference's double expression (traces bit-identical to the reference)
+    exact = None
+    if (args.storage or "f32") == "f32" and not args.no_fused:
+        prop.set_storage("f32exact")
+        for _ in range(2):  # warm-up, including the tuner for this storage
+            device_step()
+        prop.synchronize()
+        xev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)]
+               for _ in range(2)]
+        for k in range(2):
+            device_step(xev[k])
+        prop.synchronize()
+        x_ms = [sum(e[i].elapsed_time(e[i + 1]) for e in xev) / 2
+                for i in range(3)]
+        exact = {"value": round(cells_per_step / (sum(x_ms) / 1e3) / 1e9, 3),
+                 "unit": "Gcell-updates/s", "steps": 2,
+                 "forward_ms": round(x_ms[0], 2), "source_ms": round(x_ms[1], 2),
+                 "adjoint_ms": round(x_ms[2], 2),
+                 "arith": "FP32 reference order, Born coupling as the "
+                          "reference's double expression (born_set_storage "
+                          "BORN_STORE_F32_EXACT; traces bit-identical)"}
+        prop.set_storage("f32")
+
     # roofline of the dominant kernel: the fused RTM adjoint step
     peak, peak_kind = measured_peak()
     adj_launch_ms = adj_ms / nt
@@ -467,6 +491,7 @@ def run_gpu_arm(args):
             "tile_ms_per_launch": tile_ms,
             "clocks": clk.summary(), "gpu_launches": launches,
             "e2e": e2e, "cpu_baseline": cpu, "fused_fma": fused,
+            "exact_coupling": exact,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -1022,7 +1047,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fused", action="store_true",
-                    help="c2: skip the extra fused multiply-add measurement")
+                    help="c2: skip the extra fused multiply-add and exact "
+                         "coupling measurements")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 10 if args.config == "c5" else 5
