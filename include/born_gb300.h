@@ -470,6 +470,13 @@ long long born_kernel_launches(const born_handle *h);
  * and falls back to double for the few cells the test cannot decide.  Every
  * other step is the BORN_STORE_F32 one. */
 #define BORN_STORE_F32_EXACT 4
+/* The exact coupling's arithmetic on device arrays of n values:
+ * out[i] = (float)((double)r[i] + 1e-6 * (double)s[i] * (double)m[i]), as
+ * the rtm forward step under BORN_STORE_F32_EXACT forms it (two cells per
+ * thread); for testing that arithmetic on chosen inputs.  Enqueued on
+ * `stream` (a cudaStream_t; null for the legacy default stream). */
+int born_couple_exact_device(const float *r, const float *s, const float *m,
+                             float *out, long long n, void *stream);
 int born_set_storage(born_handle *h, int storage);
 int born_get_storage(const born_handle *h);
 /* Raw CUDA stream of the handle (cudaStream_t), for event timing. */

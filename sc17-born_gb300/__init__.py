@@ -97,6 +97,8 @@ _SIGS = {
     "born_loop_tile_ms": (C.c_int, [_vp, C.c_int, _fp, C.c_int]),
     "born_tuned_zseg": (C.c_int, [_vp, C.c_int]),
     "born_set_launch_overlap": (C.c_int, [_vp, C.c_int]),
+    "born_couple_exact_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_longlong,
+                                           _vp]),
     "born_set_checkpoint_interval": (C.c_int, [_vp, C.c_int]),
     "born_set_checkpoint_storage": (C.c_int, [_vp, C.c_int]),
     "born_checkpoints_reused": (C.c_int, [_vp]),

@@ -154,6 +154,106 @@ BORN_HD float couple_fast(float r, float s, float m, bool *fell_back) {
 }
 
 #ifdef __CUDACC__
+// couple_fast on two cells at once (lanes lo, hi of a 64-bit pair), with
+// the sums and multiply-adds in packed FP32 pairs (each lane rounds as the
+// scalar operation).  The products whose results feed an add (vh, and the
+// scalings of r) stay scalar: the compiler contracts a packed multiply
+// feeding a packed add into a fused multiply-add, and vh must be rounded
+// before r + vh for the exact sum.  Bit 0 / 1 of the result flag: lane lo /
+// hi needs the double fallback.
+__device__ __forceinline__ unsigned long long cp_pk(float lo, float hi) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float2 cp_upk(unsigned long long v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ __forceinline__ unsigned long long cp_add(unsigned long long a,
+                                                     unsigned long long b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long cp_sub(unsigned long long a,
+                                                     unsigned long long b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long cp_mul(unsigned long long a,
+                                                     unsigned long long b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long cp_fma(unsigned long long a,
+                                                     unsigned long long b,
+                                                     unsigned long long c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+__device__ __forceinline__ float2 couple_fast2(float2 r, float2 s, float2 m,
+                                               unsigned int *fell_back) {
+  const bool sml0 = fabsf(s.x) < 0x1p-40f && fabsf(r.x) < 0x1p60f;
+  const bool sml1 = fabsf(s.y) < 0x1p-40f && fabsf(r.y) < 0x1p60f;
+  const float sc0 = sml0 ? 0x1p64f : 1.f, sc1 = sml1 ? 0x1p64f : 1.f;
+  // scalings by powers of two are exact
+  const unsigned long long S = cp_mul(cp_pk(s.x, s.y), cp_pk(sc0, sc1));
+  const float rs0 = __fmul_rn(r.x, sc0), rs1 = __fmul_rn(r.y, sc1);
+  const unsigned long long Rr = cp_pk(rs0, rs1), M = cp_pk(m.x, m.y);
+  const unsigned long long CH = cp_pk(kCHi, kCHi), CL = cp_pk(kCLo, kCLo);
+  const unsigned long long UH = cp_mul(CH, S);
+  const float2 uh = cp_upk(UH);
+  const float vh0 = __fmul_rn(uh.x, m.x), vh1 = __fmul_rn(uh.y, m.y);
+  const unsigned long long VH = cp_pk(vh0, vh1);
+  const unsigned long long NUH = cp_pk(-uh.x, -uh.y);
+  const unsigned long long UE = cp_fma(CH, S, NUH);
+  const unsigned long long UL = cp_fma(CL, S, UE);
+  const unsigned long long VE = cp_fma(UH, M, cp_pk(-vh0, -vh1));
+  const unsigned long long VL = cp_fma(UL, M, VE);
+  const unsigned long long T = cp_add(Rr, VH);
+  const unsigned long long Z = cp_sub(T, Rr);
+  const unsigned long long E =
+      cp_add(cp_sub(Rr, cp_sub(T, Z)), cp_sub(VH, Z));
+  const unsigned long long YL = cp_add(E, VL);
+  const unsigned long long RR = cp_add(T, YL);
+  const float2 t = cp_upk(T);
+  const unsigned long long D2 = cp_mul(
+      cp_pk(0x1p-43f, 0x1p-43f),
+      cp_add(cp_pk(fabsf(vh0), fabsf(vh1)), cp_pk(fabsf(t.x), fabsf(t.y))));
+  const float2 lo = cp_upk(cp_add(T, cp_sub(YL, D2)));
+  const float2 hi = cp_upk(cp_add(T, cp_add(YL, D2)));
+  const float2 R = cp_upk(RR);
+  const float inv0 = sml0 ? 0x1p-64f : 1.f, inv1 = sml1 ? 0x1p-64f : 1.f;
+  const bool ok0 = fabsf(uh.x) >= 0x1p-100f && fabsf(vh0) >= 0x1p-100f &&
+                   lo.x == R.x && hi.x == R.x &&
+                   (!sml0 || fabsf(R.x) >= 0x1p-61f);
+  const bool ok1 = fabsf(uh.y) >= 0x1p-100f && fabsf(vh1) >= 0x1p-100f &&
+                   lo.y == R.y && hi.y == R.y &&
+                   (!sml1 || fabsf(R.y) >= 0x1p-61f);
+  const bool zero0 = s.x == 0.f || m.x == 0.f;
+  const bool zero1 = s.y == 0.f || m.y == 0.f;
+  const bool keep0 = __fmul_rn(fabsf(vh0), inv0) < 0x1p-100f &&
+                     fabsf(m.x) <= 0x1p20f && fabsf(r.x) >= 0x1p-60f &&
+                     fabsf(r.x) <= 0x1p127f;
+  const bool keep1 = __fmul_rn(fabsf(vh1), inv1) < 0x1p-100f &&
+                     fabsf(m.y) <= 0x1p20f && fabsf(r.y) >= 0x1p-60f &&
+                     fabsf(r.y) <= 0x1p127f;
+  // an exact zero s or m: vh is that signed zero (scaled by a positive
+  // power of two), and r + (+-0) rounds alike in float and double
+  float2 out;
+  out.x = zero0 ? __fadd_rn(r.x, vh0) : keep0 ? r.x : __fmul_rn(R.x, inv0);
+  out.y = zero1 ? __fadd_rn(r.y, vh1) : keep1 ? r.y : __fmul_rn(R.y, inv1);
+  *fell_back = (!zero0 && !keep0 && !ok0 ? 1u : 0u) |
+               (!zero1 && !keep1 && !ok1 ? 2u : 0u);
+  return out;
+}
+
 // the double fallback out of line, so that the compiler cannot turn the
 // rare branch into double arithmetic on every cell (FP64 runs at a small
 // fraction of the FP32 rate on this GPU)

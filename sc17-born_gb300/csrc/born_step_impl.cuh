@@ -890,17 +890,18 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
           if (MODE == kModeForward) {
             // Born coupling r += 1e-6 s img, then extraction from r
             if constexpr (Store<ST>::kExact) {
-              // float evaluation of every cell, the double expression out
-              // of line for the few the rounding test cannot decide
-              float4 nr = nb;
-              unsigned int slow = 0u;
-#pragma unroll
-              for (int jj = 0; jj < 4; ++jj) {
-                bool fb;
-                set_comp(nr, jj, couple::couple_fast(comp(nb, jj), comp(na, jj),
-                                                     comp(im, jj), &fb));
-                slow |= (fb ? 1u : 0u) << jj;
-              }
+              // float evaluation of every cell (two packed pairs), the
+              // double expression out of line for the few the rounding
+              // test cannot decide
+              unsigned int f0, f1;
+              const float2 c0 = couple::couple_fast2(
+                  make_float2(nb.x, nb.y), make_float2(na.x, na.y),
+                  make_float2(im.x, im.y), &f0);
+              const float2 c1 = couple::couple_fast2(
+                  make_float2(nb.z, nb.w), make_float2(na.z, na.w),
+                  make_float2(im.z, im.w), &f1);
+              float4 nr = make_float4(c0.x, c0.y, c1.x, c1.y);
+              const unsigned int slow = f0 | (f1 << 2);
               if (slow) {
                 for (int jj = 0; jj < 4; ++jj)
                   if (slow & (1u << jj))
