@@ -3,9 +3,12 @@ storage forms on the random-boundary RTM (source propagation + adjoint,
 cpu_prop.cc:56-129), emulated on the oracle's float primitives, with the
 image error against the FP64 oracle.  Forms per field: f32; p16 (each stored
 level rounded to FP16 with a power-of-two scale, as BORN_STORE_F16 stores
-it); pq16 (the level and its difference to the previous stored level, each
-16-bit with its own scale, the previous level rebuilt as P - Q).  With f32
-for both fields the emulation reproduces the oracle's image bit for bit.
+it); pq16 and qp16 (the level and its difference to the current level,
+each 16-bit with its own scale, the previous level rebuilt as P - Q; pq16
+takes the difference from the rounded new level, qp16 from the new level
+before rounding).  With f32 for both fields the emulation reproduces the
+oracle's image bit for bit.  STUDY_FORMS="s/r,..." (e.g. "f32/qp16")
+limits the runs to some (source field, receiver field) forms.
 
     python tests/storage_forms_study.py <model n> <data samples> [born]
 
@@ -58,7 +61,7 @@ class Field:
 
     def before_step(self):
         # the levels the step reads: cur = p1 as stored, old = p0 or P - Q
-        if self.form == "pq16":
+        if self.form in ("pq16", "qp16"):
             self.p0[:] = self.p1 - self.Q
 
     def after_step(self):
@@ -68,9 +71,16 @@ class Field:
         if self.form == "p16":
             self.p0[:] = q16(self.p0)
         elif self.form == "pq16":
+            # the difference of the stored levels (the previous level is
+            # rebuilt exactly as P - Q up to Q's rounding)
             newP = q16(self.p0)
             self.Q = q16(newP - self.p1)
             self.p0[:] = newP
+        elif self.form == "qp16":
+            # the difference of the new level before rounding and the stored
+            # current one (the time derivative keeps no level rounding)
+            self.Q = q16(self.p0 - self.p1)
+            self.p0[:] = q16(self.p0)
         self.p0, self.p1 = self.p1, self.p0
 
 
@@ -105,7 +115,7 @@ def run(case, form_s, form_r):
         # cpu_prop.cc:123-128: memcpy(p1, p0) after the last swap, so both
         # levels hold the level before the last
         S.p1[:] = S.p0
-        if form_s == "pq16":
+        if form_s in ("pq16", "qp16"):
             S.Q[:] = 0.0
     # rtmAdjoint (cpu_prop.cc:56-96) with rtm_zero_op's argument order:
     # src_p0 (the buffer a step overwrites) = the level before the last,
@@ -136,7 +146,7 @@ def run(case, form_s, form_r):
             Sa.after_step()
         else:
             Sa.p0, Sa.p1 = Sa.p1, Sa.p0
-            if form_s == "pq16":
+            if form_s in ("pq16", "qp16"):
                 Sa.Q = q16(Sa.p1 - Sa.p0)
     return img
 
@@ -160,8 +170,13 @@ if __name__ == "__main__":
     ref32 = po.run_case(po.PortProp(), case, which="adjoint")["image"]
     nrm = np.linalg.norm(ref)
     print("oracle f32 vs f64", np.linalg.norm(ref32 - ref) / nrm, flush=True)
-    for fs, fr in (("f32", "f32"), ("p16", "p16"), ("f32", "p16"),
-                   ("f32", "pq16"), ("pq16", "pq16")):
+    forms = (("f32", "f32"), ("p16", "p16"), ("f32", "p16"),
+             ("f32", "pq16"), ("pq16", "pq16"), ("f32", "qp16"),
+             ("qp16", "qp16"), ("qp16", "f32"))
+    if os.environ.get("STUDY_FORMS"):
+        forms = [tuple(x.split("/")) for x in
+                 os.environ["STUDY_FORMS"].split(",")]
+    for fs, fr in forms:
         t0 = time.time()
         img = run(case, fs, fr).reshape(ref.shape)
         print(f"s {fs:5s} r {fr:5s}: image rel L2 vs f64 "
