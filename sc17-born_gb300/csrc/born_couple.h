@@ -29,8 +29,6 @@
 // explicit rounding intrinsics, which are never contracted.
 #pragma once
 
-#include <cstring>
-
 #if defined(__CUDACC__)
 #define BORN_HD __host__ __device__ __forceinline__
 #else
@@ -75,25 +73,6 @@ BORN_HD float fabs_(float a) {
   return __builtin_fabsf(a);
 #endif
 }
-BORN_HD unsigned int bits(float a) {
-#ifdef __CUDA_ARCH__
-  return __float_as_uint(a);
-#else
-  unsigned int u;
-  std::memcpy(&u, &a, 4);
-  return u;
-#endif
-}
-BORN_HD float from_bits(unsigned int u) {
-#ifdef __CUDA_ARCH__
-  return __uint_as_float(u);
-#else
-  float a;
-  std::memcpy(&a, &u, 4);
-  return a;
-#endif
-}
-
 // the reference's expression, operation by operation in double
 BORN_HD float reference_double(float r, float s, float m) {
 #ifdef __CUDA_ARCH__
