@@ -3,7 +3,8 @@
 Ricker, 64x64 receivers) against the oracle on the same seeded inputs, in the
 reference's call order: source levels and RTM image bit for bit, Born traces
 within the 1e-5 relative L2 bound (the reference forms the 1e-6 Born
-coupling in double, cpu_prop.cc:220)."""
+coupling in double, cpu_prop.cc:220), and bit for bit too with the storage
+that forms the coupling as that double expression ("f32exact")."""
 import importlib.util
 import os
 
@@ -41,3 +42,11 @@ def test_c1_full_size_against_oracle(born, po):
     e = rel(got["traces"], want["traces"])
     print(f"c1 traces rel L2 {e:.2e}")
     assert e <= 1e-5, e
+    nz, ny, nx = case["shape"]
+    prop = born.Gb300Prop()
+    prop.createSpace(case["d"], case["d"], case["d"], 50, .0005, .0005, nx,
+                     ny, nz)
+    prop.set_storage("f32exact")
+    got = po.run_case(prop, case)
+    for k in ("src_p0", "src_p1", "image", "traces"):
+        assert np.array_equal(got[k], want[k]), (k, rel(got[k], want[k]))
