@@ -233,3 +233,38 @@ def test_bounded_wait_gives_up_with_status_and_handle_stays_usable(gpu, po):
     assert prop.lib.born_selftest_wait_timeout(prop.h) == -5
     assert prop.lib.born_synchronize(prop.h) == 0  # error word cleared
     check(po.run_case(prop, c), po.run_case(po.PortProp(), c))
+
+
+@pytest.mark.parametrize("storage", ["f32", "f32exact"])
+def test_points_on_the_interior_corners(gpu, po, storage):
+    """Sources and receivers on the outermost interior cells (x, y, z = 4
+    and n - 5: the taper, the tile and segment edges and the halo meet
+    there), some cells holding several points, jt = 2, against the oracle:
+    levels and image bit for bit, traces within the bound (bit for bit with
+    the exact coupling)."""
+    shape = (28, 36, 40)
+    c = cases.make_case(97, shape=shape, nt=61, jt=2, sinc=po.sinc_table)
+    nz, ny, nx = shape
+    corners = [x + y * nx + z * nx * ny
+               for z in (4, nz - 5) for y in (4, ny - 5) for x in (4, nx - 5)]
+    # 8 corners, then 4 of them again (points sharing a cell)
+    locs_r = np.array(corners + corners[:4], np.int32)
+    c["locs_r"] = locs_r
+    c["rec_nx"], c["rec_ny"] = 4, 3
+    rng = np.random.default_rng(98)
+    rec = np.zeros((12, c["nt_big"]), np.float32)
+    rec[:, 4:-4] = 1e-3 * rng.standard_normal((12, c["nt_big"] - 8))
+    c["rec_in"] = rec
+    # the 9 sources: 6 corners and 3 of them again
+    c["locs_s"] = np.array(corners[:6] + corners[:3], np.int32)
+    prop = gpu.Gb300Prop()
+    prop.createSpace(c["d"], c["d"], c["d"], 50, .0005, .0005, nx, ny, nz)
+    prop.set_storage(storage)
+    got = po.run_case(prop, c)
+    want = po.run_case(po.PortProp(), c)
+    assert np.linalg.norm(want["image"]) > 0
+    assert np.linalg.norm(want["traces"]) > 0
+    if storage == "f32exact":
+        check(got, want, exact=("src_p0", "src_p1", "image", "traces"))
+    else:
+        check(got, want)
