@@ -290,6 +290,14 @@ int born_op_create(born_handle *h, const born_op_params *p,
 int born_op_destroy(born_op *op);
 int born_op_sizes(const born_op *op, long long *model_n, long long *data_n,
                   int *nt_fd, float *dt_fd);
+/* Exact mode keeps each shot's background checkpoints across operator
+ * applications (the background does not depend on the model), as many
+ * shots as fit while a quarter of the device memory stays free, so a
+ * shot's adjoint after its linearised forward skips the checkpoint sweep.
+ * born_op_checkpoint_shots: shots holding checkpoints;
+ * born_op_checkpoints_reused: shot adjoints that skipped their sweep. */
+int born_op_checkpoint_shots(const born_op *op);
+long long born_op_checkpoints_reused(const born_op *op);
 int born_op_forward(born_op *op, int add, const float *model, float *data);
 int born_op_adjoint(born_op *op, int add, float *model, const float *data);
 /* FP64 dot product of two device float vectors (block partials in double),

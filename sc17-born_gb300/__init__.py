@@ -99,6 +99,8 @@ _SIGS = {
     "born_set_launch_overlap": (C.c_int, [_vp, C.c_int]),
     "born_couple_exact_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_longlong,
                                            _vp]),
+    "born_op_checkpoint_shots": (C.c_int, [_vp]),
+    "born_op_checkpoints_reused": (C.c_longlong, [_vp]),
     "born_set_checkpoint_interval": (C.c_int, [_vp, C.c_int]),
     "born_set_checkpoint_storage": (C.c_int, [_vp, C.c_int]),
     "born_checkpoints_reused": (C.c_int, [_vp]),
@@ -729,6 +731,16 @@ class BornOperator(Handle):
             self.op, C.c_void_p(a.data_ptr()), C.c_void_p(b.data_ptr()),
             a.numel(), C.byref(out))))
         return out.value
+
+    @property
+    def checkpoint_shots(self) -> int:
+        """Shots whose background checkpoints the operator keeps (exact)."""
+        return int(self.lib.born_op_checkpoint_shots(self.op))
+
+    @property
+    def checkpoints_reused(self) -> int:
+        """Shot adjoints that reused kept checkpoints instead of a sweep."""
+        return int(self.lib.born_op_checkpoints_reused(self.op))
 
     def cg(self, data, model, niter):
         """Least squares by cgstep CG; model is updated in place."""

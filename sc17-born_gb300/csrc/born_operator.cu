@@ -265,6 +265,25 @@ struct born_op {
   // the handle's background generation when it was selected
   int cur_shot = -1;
   unsigned long long cur_gen = 0;
+  // Exact mode: each shot's background checkpoints, kept across operator
+  // applications.  The background s of a shot depends only on the fixed
+  // background velocity and the shot's source, not on the model, so after
+  // a shot's linearised forward its adjoint (and every later one) can skip
+  // the forward sweep that would store them again; with one handle for all
+  // shots the handle's own checkpoints only ever belong to the last shot.
+  // A shot gets a slot while free device memory stays above a quarter of
+  // the device; the slot's buffers are the handle's checkpoint buffers
+  // while that shot's linearised forward or adjoint runs.
+  struct CkptSlot {
+    bool owned = false;
+    float *buf = nullptr, *scale = nullptr;
+    size_t bytes = 0, scale_levels = 0;
+    bool valid = false;
+    int jt = 0, nt = 0, interval = 0, kind = 0;
+  };
+  std::vector<CkptSlot> slots;
+  CkptSlot own;  // the handle's own checkpoint state while a slot is in
+  long long ckpt_reused_shots = 0;  // adjoints that skipped their sweep
 };
 
 namespace {
@@ -307,6 +326,73 @@ int op_select_shot(born_op *op, int ishot) {
   return BORN_OK;
 }
 
+// Puts shot s's checkpoint slot into the handle (false: the shot has none
+// and the handle's own checkpoints are used).
+bool op_ckpt_swap_in(born_op *op, int s) {
+  born_handle *h = op->h;
+  born_op::CkptSlot &sl = op->slots[s];
+  if (!sl.owned) {
+    const int interval =
+        op->p.ckpt_interval > 0 ? op->p.ckpt_interval : 50;
+    const size_t levels = 2 * (size_t)((op->nt + interval - 1) / interval + 1);
+    const size_t esize = h->ckpt_storage == BORN_CKPT_F16 ? 2 : 4;
+    const size_t need = levels * (size_t)h->n123 * esize;
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess ||
+        need + total_b / 4 > free_b)
+      return false;
+    sl.owned = true;  // its buffers come from the handle's allocator
+  }
+  born_op::CkptSlot &o = op->own;
+  o.buf = h->ckpt;
+  o.bytes = h->ckpt_bytes;
+  o.scale = h->ckpt_scale;
+  o.scale_levels = h->ckpt_scale_levels;
+  o.valid = h->ckpt_valid && h->ckpt_gen == h->bg_gen;
+  o.jt = h->ckpt_jt;
+  o.nt = h->ckpt_nt;
+  o.interval = h->ckpt_interval;
+  o.kind = h->ckpt_kind;
+  h->ckpt = sl.buf;
+  h->ckpt_bytes = sl.bytes;
+  h->ckpt_scale = sl.scale;
+  h->ckpt_scale_levels = sl.scale_levels;
+  // the shot's background is the same as when the slot was filled
+  h->ckpt_valid = sl.valid;
+  h->ckpt_gen = h->bg_gen;
+  h->ckpt_jt = sl.jt;
+  h->ckpt_nt = sl.nt;
+  h->ckpt_interval = sl.interval;
+  h->ckpt_kind = sl.kind;
+  return true;
+}
+
+// Takes shot s's checkpoints back from the handle (the handle's allocator
+// may have replaced the buffers) and restores the handle's own.
+void op_ckpt_swap_out(born_op *op, int s) {
+  born_handle *h = op->h;
+  born_op::CkptSlot &sl = op->slots[s];
+  sl.buf = h->ckpt;
+  sl.bytes = h->ckpt_bytes;
+  sl.scale = h->ckpt_scale;
+  sl.scale_levels = h->ckpt_scale_levels;
+  sl.valid = h->ckpt_valid && h->ckpt_gen == h->bg_gen;
+  sl.jt = h->ckpt_jt;
+  sl.nt = h->ckpt_nt;
+  sl.interval = h->ckpt_interval;
+  sl.kind = h->ckpt_kind;
+  const born_op::CkptSlot &o = op->own;
+  h->ckpt = o.buf;
+  h->ckpt_bytes = o.bytes;
+  h->ckpt_scale = o.scale;
+  h->ckpt_scale_levels = o.scale_levels;
+  h->ckpt_valid = false;  // another shot's background is in the levels now
+  h->ckpt_jt = o.jt;
+  h->ckpt_nt = o.nt;
+  h->ckpt_interval = o.interval;
+  h->ckpt_kind = o.kind;
+}
+
 int op_dot(born_op *op, const float *a, const float *b, long long n,
            double *out) {
   born_handle *h = op->h;
@@ -338,6 +424,7 @@ int born_op_create(born_handle *h, const born_op_params *p,
   born_op *op = new born_op();
   op->h = h;
   op->p = *p;
+  op->slots.resize(p->nshots);
   const long long nm = (long long)p->n1 * p->n2 * p->n3;
   op->model_n = nm;
   op->host_vel.assign(velocity, velocity + nm);
@@ -448,6 +535,10 @@ int born_op_destroy(born_op *op) {
   cudaSetDevice(op->h->device);
   cudaStreamSynchronize(op->h->stream);
   for (float *v : op->vrand) cudaFree(v);
+  for (born_op::CkptSlot &sl : op->slots) {
+    cudaFree(sl.buf);
+    cudaFree(sl.scale);
+  }
   cudaFree(op->vnone);
   cudaFree(op->traces_tmp);
   cudaFree(op->shot_tmp);
@@ -455,6 +546,17 @@ int born_op_destroy(born_op *op) {
   cudaFree(op->dot_out);
   delete op;
   return BORN_OK;
+}
+
+long long born_op_checkpoints_reused(const born_op *op) {
+  return op ? op->ckpt_reused_shots : BORN_EINVAL;
+}
+
+int born_op_checkpoint_shots(const born_op *op) {
+  if (!op) return BORN_EINVAL;
+  int n = 0;
+  for (const born_op::CkptSlot &sl : op->slots) n += sl.owned && sl.buf ? 1 : 0;
+  return n;
 }
 
 int born_op_sizes(const born_op *op, long long *model_n, long long *data_n,
@@ -490,8 +592,13 @@ int born_op_forward(born_op *op, int add, const float *model, float *data) {
     h->have_refl = true;
     OPCK(op, cudaMemsetAsync(h->rec.traces, 0, (size_t)ntr * op->nt_big * 4,
                              h->stream));
-    rc = p.exact ? born_lin_forward(h, op->jt, op->nt, nullptr)
-                 : born_rtm_forward(h, op->jt, op->nt, nullptr);
+    if (p.exact) {
+      const bool slot = op_ckpt_swap_in(op, s);
+      rc = born_lin_forward(h, op->jt, op->nt, nullptr);
+      if (slot) op_ckpt_swap_out(op, s);
+    } else {
+      rc = born_rtm_forward(h, op->jt, op->nt, nullptr);
+    }
     if (rc) return rc;
     // data += deriv(map_data(traces)) (rtm_zero_op_3d.cc:187-193)
     k_map_fwd<<<grid_for(op->shot_n), kThreads, 0, h->stream>>>(
@@ -529,9 +636,14 @@ int born_op_adjoint(born_op *op, int add, float *model, const float *data) {
     OPCK(op, cudaGetLastError());
     h->launches += 2;
     if (p.exact) {
+      const bool slot = op_ckpt_swap_in(op, s);
       rc = born_lin_adjoint(h, op->jt, op->nt,
                             p.ckpt_interval > 0 ? p.ckpt_interval : 50,
                             nullptr);
+      if (slot) {
+        if (h->ckpt_reused) op->ckpt_reused_shots++;
+        op_ckpt_swap_out(op, s);
+      }
     } else {
       rc = born_source_prop(h, op->jt, op->nt, nullptr, nullptr);
       if (!rc) rc = born_rtm_adjoint(h, op->jt, op->nt, 1, nullptr);

@@ -298,3 +298,32 @@ def test_operator_orders_after_torch_stream(born, torch_cuda):
         assert torch.equal(got_d, want_d)
         assert torch.equal(got_m, want_m)
         assert got_dot == want_dot
+
+
+def test_exact_operator_keeps_shot_checkpoints(born, torch_cuda):
+    """Exact mode keeps every shot's background checkpoints across operator
+    applications: after a linearised forward of all shots, the adjoint of
+    each shot skips its checkpoint sweep, and gives the same model as an
+    operator whose adjoint had to sweep."""
+    torch = torch_cuda
+    kw = setup_problem(seed=12, nshots=3)
+    g = torch.Generator(device="cuda").manual_seed(1006)
+    d = torch.randn(born.BornOperator(exact=True, ckpt_interval=13,
+                                      **kw).data_shape,
+                    device="cuda", generator=g)
+    fresh = born.BornOperator(exact=True, ckpt_interval=13, **kw)
+    want = torch.zeros(fresh.model_shape, device="cuda")
+    fresh.adjoint(False, want, d)   # every shot sweeps
+    assert fresh.checkpoints_reused == 0
+    op = born.BornOperator(exact=True, ckpt_interval=13, **kw)
+    m = torch.randn(op.model_shape, device="cuda", generator=g)
+    out = torch.zeros(op.data_shape, device="cuda")
+    op.forward(False, m, out)
+    assert op.checkpoint_shots == 3
+    got = torch.zeros(op.model_shape, device="cuda")
+    op.adjoint(False, got, d)
+    assert op.checkpoints_reused == 3
+    assert torch.equal(got, want)
+    op.adjoint(False, got, d)   # and again, without a forward in between
+    assert op.checkpoints_reused == 6
+    assert torch.equal(got, want)
