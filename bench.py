@@ -8,16 +8,20 @@ the RTM adjoint (sourceProp + rtmAdjoint) of configuration c2 (256^3 model,
   e2e    the same metric through the reference-facing C ABI
          (gpu_funcs_3d.h names) with pinned host buffers, host<->device
          copies inside the timed region, in the call order of
-         rtm_zero_op_3d.cc
+         rtm_zero_op_3d.cc (host_call_ms: each entry point's wall time)
   roofline  achieved GB/s of the dominant kernel (the fused RTM adjoint
          step) against the measured HBM copy bandwidth, and (stream_mix)
          against what plain streaming sustains for the step's own 7 read
          and 3 written arrays
   shot_steps_per_s  time steps of whole shots (Born forward + RTM adjoint)
          per second, over all ranks
-  tile_ms_per_launch  per-tile time per launch of each step as the time
-         loops measured them on their own steps (the chosen tile in
-         tile_cfg)
+  tile_ms_per_launch  per-tile time per launch of each step (with its
+         best z segmentation) as the time loops measured them on their own
+         steps (the chosen tile in tile_cfg, its z-segment depth in
+         tile_zseg)
+  fused_fma, exact_coupling  the same loops with fused multiply-add
+         arithmetic, and with the Born coupling formed exactly as the
+         reference's double expression (bit-identical traces)
   cpu_baseline  the oracle (C restatement of the reference cpuProp) on the
          host cores, on a bounded sample of the same workload
 
