@@ -14,8 +14,7 @@
 //     reflectivity), one TX x TY tile each.
 // A plane's centre is thus read twice (z ring, then inside its box four
 // planes later, from L2), which keeps the shared memory per CTA small enough
-// for three 128-thread CTAs per SM (four for the forward step, whose ring
-// is two stages deep).
+// for three 128-thread CTAs per SM.
 // The stencil's neighbour sums and running sums, the leapfrog and the
 // imaging adds run on packed FP32 pairs (add/sub.rn.f32x2: two cells per
 // instruction, each lane rounded like the scalar form); the products of the
@@ -147,7 +146,8 @@ constexpr unsigned int kErrWaitTimeout = 1u;
 constexpr int kZStages = 3;  // largest z-window ring depth (planes ahead)
 // z-ring depth of a mode (at most kZStages)
 constexpr int z_stages(int mode) {
-  return mode == kModeForward ? 3 : mode == kModeSource ? 3 : 3;
+  (void)mode;
+  return kZStages;
 }
 constexpr int kOStages = 3;  // largest output ring depth (planes 2 ahead)
 // output ring depth of a mode (at most kOStages).  The forward step ran

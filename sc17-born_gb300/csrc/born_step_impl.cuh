@@ -592,6 +592,8 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t zbars[kZStages];
   __shared__ __align__(8) uint64_t obars[kOStages];  // the first LY::kOSt
+  // copies issued per ring stage (the abort path waits for the last one)
+  __shared__ unsigned int s_nz[kZStages], s_no[kOStages];
   __shared__ int abort_flag;
   __shared__ float s_bound[kNBound];
   __shared__ StepScales s_sc;
@@ -630,6 +632,8 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   if (tid == 0) {
     for (int s = 0; s < LY::kZSt; ++s) mbar_init(&zbars[s], 1);
     for (int s = 0; s < LY::kOSt; ++s) mbar_init(&obars[s], 1);
+    for (int s = 0; s < kZStages; ++s) s_nz[s] = 0u;
+    for (int s = 0; s < kOStages; ++s) s_no[s] = 0u;
     // a wait elsewhere already gave up: the whole CTA leaves untouched
     abort_flag = *reinterpret_cast<volatile unsigned int *>(p.err) != 0u;
     mbar_fence_init();
@@ -683,6 +687,7 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   auto issue_z = [&](int k) {
     const int plane = z0 - kRadius + k;
     const int st = k % LY::kZSt;
+    ++s_nz[st];
     mbar_expect_tx(&zbars[st], LY::kZTx);
     unsigned char *dst = zring + st * LY::kZStage;
     if (M::kBoxA) tma_load_3d(dst, &maps.zc_a, xz, y0, plane, &zbars[st]);
@@ -693,6 +698,7 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   auto issue_out = [&](int j) {
     const int plane = z0 + j;
     const int st = j % LY::kOSt;
+    ++s_no[st];
     mbar_expect_tx(&obars[st], LY::kOTx);
     unsigned char *dst = oring + st * LY::kOStage;
     if (M::kBoxA)
@@ -958,11 +964,14 @@ __device__ __forceinline__ void step_body(const StepMaps *mp,
   }
 
   if (abort_flag && tid == 0) {
-    // drain whatever is still in flight (bounded) before the CTA retires
+    // wait (bounded) for the last copy issued into each ring stage before
+    // the CTA retires; thread 0 is the only issuer, so the counts are final
     for (int s = 0; s < LY::kZSt + LY::kOSt; ++s) {
       uint64_t *b = s < LY::kZSt ? &zbars[s] : &obars[s - LY::kZSt];
+      const unsigned int n = s < LY::kZSt ? s_nz[s] : s_no[s - LY::kZSt];
+      if (n == 0u) continue;
       const uint64_t t0 = global_ns();
-      while (!mbar_try_wait(b, 0) && !mbar_try_wait(b, 1) &&
+      while (!mbar_try_wait(b, (n - 1u) & 1u) &&
              global_ns() - t0 < 100000000ull) {
       }
     }
