@@ -97,6 +97,8 @@ _SIGS = {
     "born_loop_tile_ms": (C.c_int, [_vp, C.c_int, _fp, C.c_int]),
     "born_tuned_zseg": (C.c_int, [_vp, C.c_int]),
     "born_set_launch_overlap": (C.c_int, [_vp, C.c_int]),
+    "born_set_host_prewarm": (C.c_int, [_vp, C.c_int]),
+    "born_host_prewarm_count": (C.c_longlong, [_vp]),
     "born_couple_exact_device": (C.c_int, [_vp, _vp, _vp, _vp, C.c_longlong,
                                            _vp]),
     "born_op_checkpoint_shots": (C.c_int, [_vp]),
@@ -283,6 +285,10 @@ class Handle:
     def set_launch_overlap(self, enable: bool = True):
         """Programmatic dependent launch of the time steps (default on)."""
         self.check(self.lib.born_set_launch_overlap(self.h, int(enable)))
+
+    def set_host_prewarm(self, enable: bool = True):
+        """Warm the closing host copies during the loops (default on)."""
+        self.check(self.lib.born_set_host_prewarm(self.h, int(enable)))
 
     def autotune(self, enable: bool = True):
         self.check(self.lib.born_autotune(self.h, int(enable)))

@@ -83,6 +83,15 @@ struct born_handle {
   // step launches overlap the previous step's tail (programmatic dependent
   // launch); born_set_launch_overlap
   bool overlap = true;
+  // closing device-to-host copies of a time loop into page-locked host
+  // arrays: a first copy into the same array on `side` while the loop runs
+  // (born_set_host_prewarm); `prewarm_pending` while the closing copy has
+  // not been ordered after it
+  bool prewarm = true;
+  bool prewarm_pending = false;
+  long long prewarm_copies = 0;
+  cudaStream_t side = nullptr;
+  cudaEvent_t side_go = nullptr, side_done = nullptr;
   // bumped whenever device buffers or point sets are reallocated, so that
   // cached descriptors and graphs built over them can notice
   unsigned long long generation = 0;
