@@ -17,7 +17,9 @@ HEADERS = [os.path.join(ROOT, "include", "born_gb300.h"),
 def declared_functions(path):
     text = open(path).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?[a-z_]+\s*\**\s*\**([a-z_0-9]+)\(",
+    # return types of one or more words (long long, unsigned int, ...)
+    names = re.findall(r"^\s*(?:const\s+)?(?:(?:unsigned|signed|long|short)"
+                       r"\s+)*[a-z_]+(?:\s+|\s*\*+\s*)([a-z_0-9]+)\(",
                        text, flags=re.M)
     return sorted(set(names))
 
