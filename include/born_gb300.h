@@ -420,9 +420,9 @@ int born_set_launch_overlap(born_handle *h, int enable);
  * then overwrites every byte with the result.  The first copy into such an
  * array after other host arrays were copied took 2-24 ms per 199 MB on
  * GB300, against 0.96 ms for the next one; the warming copy takes that cost
- * off the loop's critical path.  The destination's contents during the call
- * are undefined (they are the result once it returns); enable = 0 leaves it
- * untouched until the closing copy. */
+ * off the loop's critical path.  The destination's contents are undefined
+ * during the call and after a failed one (a successful call leaves the
+ * result); enable = 0 leaves it untouched until the closing copy. */
 int born_set_host_prewarm(born_handle *h, int enable);
 /* Warming copies made so far by the handle. */
 long long born_host_prewarm_count(const born_handle *h);
